@@ -1,0 +1,625 @@
+// extern "C" entry points of libegx.so (declared in include/egx.h).
+#include <complex>
+#include <cstring>
+#include <map>
+#include <memory>
+
+#include "egx_green.cuh"
+#include "egx_krylov.cuh"
+#include "egx_operator.cuh"
+
+using namespace egx;
+typedef std::complex<double> cd;
+
+struct egx_green {
+    int nx = 0, ny = 0, nz = 0;
+    DevBuf g64;  // quadrant, complex128
+    DevBuf g32;  // quadrant, complex64 (mixed precision)
+    bool has32 = false;
+};
+
+struct egx_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    long launches = 0;
+
+    // prepared operator
+    egx_green *g = nullptr;
+    int type = -1;
+    int nx = 0, ny = 0, nz = 0;
+    DevBuf r64, fwd64, bwd64, r32, fwd32, bwd32;
+    bool prepared32 = false;
+    DevBuf buf64, buf32;
+    // FFT twiddles for the operator sizes
+    int tw_n0 = 0, tw_n1 = 0;
+    DevBuf tw0_64, tw1_64, tw0_32, tw1_32;
+    FftPlan p0{}, p1{};
+    // host staging
+    DevBuf xin, yout, xin32, yout32;
+    // solvers (cached workspaces)
+    std::unique_ptr<Gmres<double>> outer64, inner64;
+    std::unique_ptr<Gmres<float>> outer32, inner32;
+    std::string key64, key32;
+    // preconditioner plug
+    int precond_kind = EGX_PRECOND_GMRES;
+    egx_precond_fn precond_fn = nullptr;
+    void *precond_user = nullptr;
+    // FFT scratch for egx_fft2d
+    DevBuf fftbuf;
+    // mixed-solve workspace
+    DevBuf nrm_part, nrm_out, mix_r, mix_t, mix_r32, mix_d32;
+    std::map<int, std::pair<std::shared_ptr<DevBuf>, FftPlan>> tw_cache;
+};
+
+namespace {
+
+int fail(egx_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+#define EGX_GUARD(ctx, ...)                                             \
+    try {                                                               \
+        __VA_ARGS__;                                                    \
+        return EGX_OK;                                                  \
+    } catch (const egx::Error &e) {                                     \
+        return fail((ctx), e.code, e.what());                           \
+    } catch (const std::exception &e) {                                 \
+        return fail((ctx), EGX_ERR_INVALID, e.what());                  \
+    }
+
+void set_device(egx_ctx *ctx) { EGX_CUDA(cudaSetDevice(ctx->device)); }
+
+// Device copy of the twiddle table for length n in precision T.
+template <typename T>
+void upload_twiddles(DevBuf &dst, int n, cudaStream_t s) {
+    std::vector<double> t = twiddles(n);
+    if (sizeof(T) == sizeof(double)) {
+        dst.ensure(t.size() * sizeof(double));
+        EGX_CUDA(cudaMemcpyAsync(dst.p, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        EGX_CUDA(cudaStreamSynchronize(s));
+    } else {
+        std::vector<float> f(t.begin(), t.end());
+        dst.ensure(f.size() * sizeof(float));
+        EGX_CUDA(cudaMemcpyAsync(dst.p, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+        EGX_CUDA(cudaStreamSynchronize(s));
+    }
+}
+
+void ensure_twiddles(egx_ctx *ctx, int n0, int n1) {
+    if (ctx->tw_n0 == n0 && ctx->tw_n1 == n1) return;
+    ctx->p0 = make_fft_plan(n0);
+    ctx->p1 = make_fft_plan(n1);
+    upload_twiddles<double>(ctx->tw0_64, n0, ctx->stream);
+    upload_twiddles<double>(ctx->tw1_64, n1, ctx->stream);
+    upload_twiddles<float>(ctx->tw0_32, n0, ctx->stream);
+    upload_twiddles<float>(ctx->tw1_32, n1, ctx->stream);
+    ctx->tw_n0 = n0;
+    ctx->tw_n1 = n1;
+}
+
+long nvec(const egx_ctx *ctx) { return (long)ctx->nx * ctx->ny * 3 * ctx->nz; }
+
+template <typename T>
+void apply_dev(egx_ctx *ctx, const C<T> *x, C<T> *y, int nrhs) {
+    EGX_CHECK(ctx->g && ctx->type >= 0, EGX_ERR_STATE, "operator is not prepared (PrepareOperator not called)");
+    OpDims d{ctx->nx, ctx->ny, ctx->nz, nrhs, nrhs * 3 * ctx->nz, nvec(ctx)};
+    size_t bufbytes = (size_t)4 * ctx->nx * ctx->ny * d.B * sizeof(C<T>);
+    const bool dbl = sizeof(T) == sizeof(double);
+    DevBuf &buf = dbl ? ctx->buf64 : ctx->buf32;
+    buf.ensure(bufbytes);
+    OperatorData<T> op;
+    if (dbl) {
+        op.r = (const C<T> *)ctx->r64.p;
+        op.fwd = (const C<T> *)ctx->fwd64.p;
+        op.bwd = (const C<T> *)ctx->bwd64.p;
+    } else {
+        EGX_CHECK(ctx->g->has32 && ctx->prepared32, EGX_ERR_STATE, "complex64 operator is not available");
+        op.r = (const C<T> *)ctx->r32.p;
+        op.fwd = (const C<T> *)ctx->fwd32.p;
+        op.bwd = (const C<T> *)ctx->bwd32.p;
+    }
+    op.type = ctx->type;
+    const C<T> *G = dbl ? (const C<T> *)ctx->g->g64.p : (const C<T> *)ctx->g->g32.p;
+    const C<T> *tw0 = dbl ? (const C<T> *)ctx->tw0_64.p : (const C<T> *)ctx->tw0_32.p;
+    const C<T> *tw1 = dbl ? (const C<T> *)ctx->tw1_64.p : (const C<T> *)ctx->tw1_32.p;
+    operator_apply<T>(d, op, G, x, y, buf.as<C<T>>(), tw0, tw1, ctx->p0, ctx->p1, ctx->stream, &ctx->launches);
+}
+
+// Quadrant point (a, b) <- reference layout point (a, b).
+void gather_quadrant(int nx, int ny, int nz, const double *const comps[6], std::vector<cd> &q) {
+    GreenDims gd{nx, ny, nz};
+    const int S = gd.S(), A = gd.A(), Bs = gd.Bs();
+    q.assign((size_t)gd.Q() * Bs, cd(0, 0));
+    const int blk[6] = {S, S, S, S, A, A};
+    const int off[6] = {0, S, 2 * S, 3 * S, 4 * S, 4 * S + A};
+    for (int a = 0; a <= nx; a++)
+        for (int b = 0; b <= ny; b++) {
+            long qi = (long)a * (ny + 1) + b;
+            long pt = (long)a * 2 * ny + b;
+            for (int c = 0; c < 6; c++) {
+                const cd *src = reinterpret_cast<const cd *>(comps[c]) + pt * blk[c];
+                std::memcpy(&q[qi * Bs + off[c]], src, sizeof(cd) * blk[c]);
+            }
+        }
+}
+
+}  // namespace
+
+extern "C" {
+
+int egx_version(void) { return 1; }
+
+int egx_create(int device, egx_ctx **out) {
+    if (!out) return EGX_ERR_INVALID;
+    *out = nullptr;
+    auto *ctx = new egx_ctx();
+    ctx->device = device;
+    try {
+        set_device(ctx);
+        EGX_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        ctx->own_stream = true;
+    } catch (const egx::Error &e) {
+        delete ctx;
+        return e.code;
+    }
+    *out = ctx;
+    return EGX_OK;
+}
+
+int egx_destroy(egx_ctx *ctx) {
+    if (!ctx) return EGX_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->outer64.reset();
+    ctx->inner64.reset();
+    ctx->outer32.reset();
+    ctx->inner32.reset();
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return EGX_OK;
+}
+
+int egx_last_error(egx_ctx *ctx, char *buf, size_t len) {
+    if (!ctx || !buf || len == 0) return EGX_ERR_INVALID;
+    std::strncpy(buf, ctx->err.c_str(), len - 1);
+    buf[len - 1] = 0;
+    return EGX_OK;
+}
+
+int egx_set_stream(egx_ctx *ctx, void *stream) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        set_device(ctx);
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+        ctx->stream = (cudaStream_t)stream;
+        ctx->own_stream = false;
+        ctx->outer64.reset();
+        ctx->inner64.reset();
+        ctx->outer32.reset();
+        ctx->inner32.reset();
+        ctx->key64.clear();
+        ctx->key32.clear();
+    });
+}
+
+long egx_launch_count(egx_ctx *ctx) {
+    if (!ctx) return -1;
+    long n = ctx->launches;
+    if (ctx->outer64) n += ctx->outer64->kernel_launches;
+    if (ctx->inner64) n += ctx->inner64->kernel_launches;
+    if (ctx->outer32) n += ctx->outer32->kernel_launches;
+    if (ctx->inner32) n += ctx->inner32->kernel_launches;
+    return n;
+}
+
+int egx_green_upload(egx_ctx *ctx, int nx, int ny, int nz, const double *const comps[6], int precision,
+                     egx_green **out) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(out && comps && nx > 0 && ny > 0 && nz > 0, EGX_ERR_INVALID, "bad Green tensor arguments");
+        for (int c = 0; c < 6; c++) EGX_CHECK(comps[c], EGX_ERR_INVALID, "null Green tensor component");
+        set_device(ctx);
+        std::vector<cd> q;
+        gather_quadrant(nx, ny, nz, comps, q);
+        auto g = std::unique_ptr<egx_green>(new egx_green());
+        g->nx = nx;
+        g->ny = ny;
+        g->nz = nz;
+        g->g64.ensure(q.size() * sizeof(cd));
+        EGX_CUDA(cudaMemcpyAsync(g->g64.p, q.data(), q.size() * sizeof(cd), cudaMemcpyHostToDevice, ctx->stream));
+        if (precision == EGX_PREC_MIXED) {
+            g->g32.ensure(q.size() * sizeof(float2));
+            convert_d2f(g->g64.as<double2>(), g->g32.as<float2>(), (long)q.size(), 1.0, ctx->stream);
+            ctx->launches++;
+            g->has32 = true;
+        }
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        *out = g.release();
+    });
+}
+
+int egx_green_download(egx_ctx *ctx, const egx_green *g, double *const comps[6]) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(g && comps, EGX_ERR_INVALID, "bad arguments");
+        set_device(ctx);
+        GreenDims gd{g->nx, g->ny, g->nz};
+        const int S = gd.S(), A = gd.A(), Bs = gd.Bs();
+        std::vector<cd> q((size_t)gd.Q() * Bs);
+        EGX_CUDA(cudaMemcpyAsync(q.data(), g->g64.p, q.size() * sizeof(cd), cudaMemcpyDeviceToHost, ctx->stream));
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        const int blk[6] = {S, S, S, S, A, A};
+        const int off[6] = {0, S, 2 * S, 3 * S, 4 * S, 4 * S + A};
+        // parity (x, y) of xx, xy, yy, zz, xz, yz
+        const int px[6] = {1, -1, 1, 1, -1, 1}, py[6] = {1, -1, 1, 1, 1, -1};
+        const int n0 = 2 * g->nx, n1 = 2 * g->ny;
+        for (int kx = 0; kx < n0; kx++)
+            for (int ky = 0; ky < n1; ky++) {
+                int a = kx <= g->nx ? kx : n0 - kx;
+                int b = ky <= g->ny ? ky : n1 - ky;
+                bool mx = kx > g->nx, my = ky > g->ny;
+                long qi = (long)a * (g->ny + 1) + b;
+                long pt = (long)kx * n1 + ky;
+                for (int c = 0; c < 6; c++) {
+                    double sg = (mx ? px[c] : 1) * (my ? py[c] : 1);
+                    cd *dst = reinterpret_cast<cd *>(comps[c]) + pt * blk[c];
+                    const cd *src = &q[qi * Bs + off[c]];
+                    for (int t = 0; t < blk[c]; t++) dst[t] = sg * src[t];
+                }
+            }
+    });
+}
+
+int egx_green_free(egx_ctx *ctx, egx_green *g) {
+    if (!ctx || !g) return EGX_ERR_INVALID;
+    if (ctx->g == g) {
+        ctx->g = nullptr;
+        ctx->type = -1;
+    }
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    delete g;
+    return EGX_OK;
+}
+
+int egx_op_prepare(egx_ctx *ctx, egx_green *g, const double *zeta, const double *zeta0, const double *dz, int type) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(g, EGX_ERR_INVALID, "greenTensor is null");
+        EGX_CHECK(zeta && zeta0 && dz, EGX_ERR_INVALID, "null model arrays");
+        EGX_CHECK(type == EGX_OP_A || type == EGX_OP_CHI0, EGX_ERR_INVALID, "unknown operator type");
+        set_device(ctx);
+        const int nx = g->nx, ny = g->ny, nz = g->nz;
+        const cd *z = reinterpret_cast<const cd *>(zeta);
+        const cd *z0 = reinterpret_cast<const cd *>(zeta0);
+        // PrepareRFunction / PrepareForwardFactors / PrepareBackwardFactors (ConvolutionOperator.cs:90-143)
+        std::vector<cd> r((size_t)nx * ny * nz), fwd(nz), bwd(nz);
+        const cd norm(1.0 / ((double)nx * (double)ny * 4), 0);
+        for (int k = 0; k < nz; k++) {
+            fwd[k] = cd(std::sqrt(z0[k].real()), 0);
+            cd sc(2 * std::sqrt(z0[k].real()), 0);
+            sc /= dz[k];
+            sc *= norm;
+            bwd[k] = sc;
+        }
+        for (long i = 0; i < (long)nx * ny; i++)
+            for (int k = 0; k < nz; k++) {
+                cd zz = z[i * nz + k];
+                cd conj0 = std::conj(z0[k]);
+                if (type == EGX_OP_CHI0) r[i * nz + k] = cd(std::sqrt(z0[k].real()), 0) / (zz + conj0);
+                else r[i * nz + k] = (zz - z0[k]) / (zz + conj0);
+            }
+        ctx->r64.ensure(r.size() * sizeof(cd));
+        ctx->fwd64.ensure(nz * sizeof(cd));
+        ctx->bwd64.ensure(nz * sizeof(cd));
+        EGX_CUDA(cudaMemcpyAsync(ctx->r64.p, r.data(), r.size() * sizeof(cd), cudaMemcpyHostToDevice, ctx->stream));
+        EGX_CUDA(cudaMemcpyAsync(ctx->fwd64.p, fwd.data(), nz * sizeof(cd), cudaMemcpyHostToDevice, ctx->stream));
+        EGX_CUDA(cudaMemcpyAsync(ctx->bwd64.p, bwd.data(), nz * sizeof(cd), cudaMemcpyHostToDevice, ctx->stream));
+        ctx->prepared32 = false;
+        if (g->has32) {
+            ctx->r32.ensure(r.size() * sizeof(float2));
+            ctx->fwd32.ensure(nz * sizeof(float2));
+            ctx->bwd32.ensure(nz * sizeof(float2));
+            convert_d2f(ctx->r64.as<double2>(), ctx->r32.as<float2>(), (long)r.size(), 1.0, ctx->stream);
+            convert_d2f(ctx->fwd64.as<double2>(), ctx->fwd32.as<float2>(), nz, 1.0, ctx->stream);
+            convert_d2f(ctx->bwd64.as<double2>(), ctx->bwd32.as<float2>(), nz, 1.0, ctx->stream);
+            ctx->launches += 3;
+            ctx->prepared32 = true;
+        }
+        ensure_twiddles(ctx, 2 * nx, 2 * ny);
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->g = g;
+        ctx->type = type;
+        ctx->nx = nx;
+        ctx->ny = ny;
+        ctx->nz = nz;
+    });
+}
+
+int egx_op_apply(egx_ctx *ctx, const double *x, double *y, int nrhs, int where) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(x && y && nrhs >= 1, EGX_ERR_INVALID, "bad apply arguments");
+        set_device(ctx);
+        EGX_CHECK(ctx->g, EGX_ERR_STATE, "operator is not prepared");
+        long n = nvec(ctx) * nrhs;
+        if (where == EGX_DEVICE) {
+            apply_dev<double>(ctx, (const double2 *)x, (double2 *)y, nrhs);
+        } else {
+            ctx->xin.ensure(n * sizeof(double2));
+            ctx->yout.ensure(n * sizeof(double2));
+            EGX_CUDA(cudaMemcpyAsync(ctx->xin.p, x, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+            apply_dev<double>(ctx, ctx->xin.as<double2>(), ctx->yout.as<double2>(), nrhs);
+            EGX_CUDA(cudaMemcpyAsync(y, ctx->yout.p, n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int egx_op_apply_c64(egx_ctx *ctx, const float *x, float *y, int nrhs, int where) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(x && y && nrhs >= 1, EGX_ERR_INVALID, "bad apply arguments");
+        set_device(ctx);
+        EGX_CHECK(ctx->g, EGX_ERR_STATE, "operator is not prepared");
+        long n = nvec(ctx) * nrhs;
+        if (where == EGX_DEVICE) {
+            apply_dev<float>(ctx, (const float2 *)x, (float2 *)y, nrhs);
+        } else {
+            ctx->xin32.ensure(n * sizeof(float2));
+            ctx->yout32.ensure(n * sizeof(float2));
+            EGX_CUDA(cudaMemcpyAsync(ctx->xin32.p, x, n * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
+            apply_dev<float>(ctx, ctx->xin32.as<float2>(), ctx->yout32.as<float2>(), nrhs);
+            EGX_CUDA(cudaMemcpyAsync(y, ctx->yout32.p, n * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int egx_fft2d(egx_ctx *ctx, double *buf, int n0, int n1, int howmany, int sign, int where) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(buf && n0 > 0 && n1 > 0 && howmany > 0, EGX_ERR_INVALID, "bad FFT arguments");
+        EGX_CHECK(sign == -1 || sign == 1, EGX_ERR_INVALID, "sign must be -1 or +1");
+        set_device(ctx);
+        FftPlan p0 = make_fft_plan(n0), p1 = make_fft_plan(n1);
+        DevBuf t0, t1;
+        upload_twiddles<double>(t0, n0, ctx->stream);
+        upload_twiddles<double>(t1, n1, ctx->stream);
+        long n = (long)n0 * n1 * howmany;
+        double2 *dbuf;
+        if (where == EGX_DEVICE) {
+            dbuf = (double2 *)buf;
+        } else {
+            ctx->fftbuf.ensure(n * sizeof(double2));
+            dbuf = ctx->fftbuf.as<double2>();
+            EGX_CUDA(cudaMemcpyAsync(dbuf, buf, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+        }
+        fft2d<double>(dbuf, n0, n1, howmany, sign, t0.as<double2>(), t1.as<double2>(), p0, p1, ctx->stream,
+                      &ctx->launches);
+        if (where != EGX_DEVICE)
+            EGX_CUDA(cudaMemcpyAsync(buf, dbuf, n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int egx_set_precond(egx_ctx *ctx, int kind, egx_precond_fn fn, void *user) {
+    if (!ctx) return EGX_ERR_INVALID;
+    if (kind != EGX_PRECOND_GMRES && kind != EGX_PRECOND_CALLBACK && kind != EGX_PRECOND_NONE)
+        return fail(ctx, EGX_ERR_INVALID, "unknown preconditioner kind");
+    if (kind == EGX_PRECOND_CALLBACK && !fn) return fail(ctx, EGX_ERR_INVALID, "callback preconditioner without fn");
+    ctx->precond_kind = kind;
+    ctx->precond_fn = fn;
+    ctx->precond_user = user;
+    return EGX_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// FGMRES with the inner GMRES preconditioner (or a callback / none) in
+// precision T on device vectors b, x (x holds the initial guess).
+template <typename T>
+GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in, double tol, int max_restarts,
+                       bool check_true, int precond_kind, int *n_applies, bool zero_guess_inner_rhs) {
+    const long n = nvec(ctx);
+    const bool dbl = sizeof(T) == sizeof(double);
+    char keybuf[128];
+    snprintf(keybuf, sizeof keybuf, "%ld/%d/%d/%g/%d/%d/%d", n, m_out, m_in, tol, max_restarts, (int)check_true,
+             precond_kind);
+    std::unique_ptr<Gmres<T>> *outer, *inner;
+    std::string *key;
+    if (dbl) {
+        outer = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->outer64);
+        inner = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->inner64);
+        key = &ctx->key64;
+    } else {
+        outer = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->outer32);
+        inner = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->inner32);
+        key = &ctx->key32;
+    }
+    if (*key != keybuf) {
+        outer->reset();
+        inner->reset();
+        outer->reset(new Gmres<T>(n, m_out, tol, max_restarts, check_true, ctx->stream));
+        if (precond_kind == EGX_PRECOND_GMRES) inner->reset(new Gmres<T>(n, m_in, tol, 1, false, ctx->stream));
+        *key = keybuf;
+    }
+    int applies = 0;
+    auto apply = [ctx, &applies](const C<T> *in, C<T> *out) {
+        apply_dev<T>(ctx, in, out, 1);
+        applies++;
+    };
+    (*outer)->apply = apply;
+    if (precond_kind == EGX_PRECOND_GMRES) {
+        (*inner)->apply = apply;
+        Gmres<T> *in = inner->get();
+        (*outer)->precond = [in](const C<T> *src, C<T> *dst) { in->solve(src, src, dst); };
+    } else if (precond_kind == EGX_PRECOND_CALLBACK) {
+        egx_precond_fn fn = ctx->precond_fn;
+        void *user = ctx->precond_user;
+        cudaStream_t s = ctx->stream;
+        const int prec = dbl ? EGX_PREC_FP64 : EGX_PREC_MIXED;
+        (*outer)->precond = [fn, user, n, s, prec](const C<T> *src, C<T> *dst) {
+            EGX_CUDA(cudaStreamSynchronize(s));
+            int rc = fn(user, src, dst, n, prec);
+            if (rc != 0) throw Error(EGX_ERR_INVALID, "preconditioner callback failed");
+        };
+    } else {
+        (*outer)->precond = nullptr;
+    }
+    (void)zero_guess_inner_rhs;
+    GmresResult r = (*outer)->solve(b, x, x);
+    *n_applies = applies;
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int egx_fgmres_solve(egx_ctx *ctx, const double *b, double *x, const egx_gmres_params *p, egx_result *res,
+                     int where) {
+    if (!ctx) return EGX_ERR_INVALID;
+    int status = EGX_OK;
+    try {
+        EGX_CHECK(b && x && p && res, EGX_ERR_INVALID, "bad solve arguments");
+        EGX_CHECK(p->m_out >= 1 && p->m_in >= 1 && p->max_restarts >= 1 && p->tol > 0, EGX_ERR_INVALID,
+                  "bad GMRES parameters");
+        set_device(ctx);
+        EGX_CHECK(ctx->g && ctx->type >= 0, EGX_ERR_STATE, "operator is not prepared");
+        const long n = nvec(ctx);
+        const double2 *db;
+        double2 *dx;
+        if (where == EGX_DEVICE) {
+            db = (const double2 *)b;
+            dx = (double2 *)x;
+        } else {
+            ctx->xin.ensure(2 * n * sizeof(double2));
+            db = ctx->xin.as<double2>();
+            dx = ctx->xin.as<double2>() + n;
+            EGX_CUDA(cudaMemcpyAsync((void *)db, b, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+            EGX_CUDA(cudaMemcpyAsync(dx, x, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+        }
+        int kind = p->precond;
+        if (kind == EGX_PRECOND_GMRES && ctx->precond_kind == EGX_PRECOND_CALLBACK) kind = EGX_PRECOND_CALLBACK;
+        int applies = 0;
+        GmresResult r = run_fgmres<double>(ctx, db, dx, p->m_out, p->m_in, p->tol, p->max_restarts,
+                                           p->check_true != 0, kind, &applies, false);
+        if (where != EGX_DEVICE)
+            EGX_CUDA(cudaMemcpyAsync(x, dx, n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        res->converged = r.converged;
+        res->iterations = r.iterations;
+        res->arnoldi_be = r.arnoldi_be;
+        res->true_be = r.true_be;
+        res->n_applies = applies;
+        res->n_refinements = 0;
+        if (!r.converged) status = fail(ctx, EGX_ERR_NOT_CONVERGED, "FGMRES did not converge");
+    } catch (const egx::Error &e) {
+        return fail(ctx, e.code, e.what());
+    } catch (const std::exception &e) {
+        return fail(ctx, EGX_ERR_INVALID, e.what());
+    }
+    return status;
+}
+
+int egx_mixed_solve(egx_ctx *ctx, const double *b, double *x, const egx_mixed_params *p, egx_result *res,
+                    int where) {
+    if (!ctx) return EGX_ERR_INVALID;
+    int status = EGX_OK;
+    try {
+        EGX_CHECK(b && x && p && res, EGX_ERR_INVALID, "bad solve arguments");
+        EGX_CHECK(p->m_out >= 1 && p->m_in >= 1 && p->max_outer >= 1 && p->tol > 0 && p->inner_tol > 0,
+                  EGX_ERR_INVALID, "bad mixed-solve parameters");
+        set_device(ctx);
+        EGX_CHECK(ctx->g && ctx->type >= 0, EGX_ERR_STATE, "operator is not prepared");
+        EGX_CHECK(ctx->g->has32 && ctx->prepared32, EGX_ERR_STATE,
+                  "mixed solve needs a Green tensor built or uploaded with EGX_PREC_MIXED");
+        const long n = nvec(ctx);
+        const double2 *db;
+        double2 *dx;
+        if (where == EGX_DEVICE) {
+            db = (const double2 *)b;
+            dx = (double2 *)x;
+        } else {
+            ctx->xin.ensure(2 * n * sizeof(double2));
+            db = ctx->xin.as<double2>();
+            dx = ctx->xin.as<double2>() + n;
+            EGX_CUDA(cudaMemcpyAsync((void *)db, b, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+            EGX_CUDA(cudaMemcpyAsync(dx, x, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+        }
+        // outer FP64 iterative refinement: r = b - A x (FP64), inner complex64
+        // FGMRES on A d = r / ||r||, x += ||r|| d.
+        DevBuf &r32 = ctx->mix_r32, &d32 = ctx->mix_d32;
+        ctx->mix_r.ensure(n * sizeof(double2));
+        ctx->mix_t.ensure(n * sizeof(double2));
+        r32.ensure(n * sizeof(float2));
+        d32.ensure(n * sizeof(float2));
+        ctx->nrm_part.ensure(2048 * sizeof(double));
+        ctx->nrm_out.ensure(sizeof(double));
+        double2 *r = ctx->mix_r.as<double2>(), *t = ctx->mix_t.as<double2>();
+        int applies64 = 0, applies32 = 0, iters = 0;
+        auto norm64 = [&](const double2 *v) {
+            DevBuf &out = ctx->nrm_out;
+            VecOps<double>::norm2(v, n, out.as<double>(), ctx->nrm_part.as<double>(), 1024, ctx->stream);
+            ctx->launches += 2;
+            double h;
+            EGX_CUDA(cudaMemcpyAsync(&h, out.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+            EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+            return std::sqrt(h);
+        };
+        double bn = norm64(db);
+        apply_dev<double>(ctx, dx, t, 1);
+        applies64++;
+        VecOps<double>::sub(db, t, r, n, ctx->stream);
+        ctx->launches++;
+        double rn = norm64(r);
+        double be = bn > 0 ? rn / bn : 0.0;
+        int k = 0;
+        bool conv = be < p->tol;
+        double last_arnoldi = -1;
+        while (!conv && k < p->max_outer) {
+            convert_d2f(r, r32.as<float2>(), n, 1.0 / rn, ctx->stream);
+            VecOps<float>::zero(d32.as<float2>(), n, ctx->stream);
+            ctx->launches += 1;
+            int a32 = 0;
+            GmresResult ir = run_fgmres<float>(ctx, r32.as<float2>(), d32.as<float2>(), p->m_out, p->m_in,
+                                               p->inner_tol, p->inner_restarts, false, EGX_PRECOND_GMRES, &a32, true);
+            applies32 += a32;
+            iters += ir.iterations;
+            last_arnoldi = ir.arnoldi_be;
+            convert_f2d_add(d32.as<float2>(), dx, n, rn, ctx->stream);
+            apply_dev<double>(ctx, dx, t, 1);
+            applies64++;
+            VecOps<double>::sub(db, t, r, n, ctx->stream);
+            ctx->launches += 2;
+            rn = norm64(r);
+            be = rn / bn;
+            k++;
+            conv = be < p->tol;
+        }
+        if (where != EGX_DEVICE)
+            EGX_CUDA(cudaMemcpyAsync(x, dx, n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        res->converged = conv;
+        res->iterations = iters;
+        res->arnoldi_be = last_arnoldi;
+        res->true_be = be;
+        res->n_applies = applies64 + applies32;
+        res->n_refinements = k;
+        if (!conv) status = fail(ctx, EGX_ERR_NOT_CONVERGED, "mixed-precision refinement did not converge");
+    } catch (const egx::Error &e) {
+        return fail(ctx, e.code, e.what());
+    } catch (const std::exception &e) {
+        return fail(ctx, EGX_ERR_INVALID, e.what());
+    }
+    return status;
+}
+
+}  // extern "C"

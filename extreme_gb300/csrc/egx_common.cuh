@@ -1,0 +1,100 @@
+// Shared definitions of the egx CUDA library: complex arithmetic on
+// double2/float2, error handling, the context object.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include <stdexcept>
+
+#include "../../include/egx.h"
+
+namespace egx {
+
+// ---------------------------------------------------------------- complex
+template <typename T> struct cvec;
+template <> struct cvec<double> { typedef double2 type; };
+template <> struct cvec<float> { typedef float2 type; };
+
+template <typename T> using C = typename cvec<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ C<T> mk(T re, T im) { C<T> r; r.x = re; r.y = im; return r; }
+template <typename T> __host__ __device__ __forceinline__ C<T> cadd(C<T> a, C<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
+template <typename T> __host__ __device__ __forceinline__ C<T> csub(C<T> a, C<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }
+template <typename T> __host__ __device__ __forceinline__ C<T> cmul(C<T> a, C<T> b) {
+    return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T> __host__ __device__ __forceinline__ C<T> cscale(C<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
+template <typename T> __host__ __device__ __forceinline__ C<T> cconj(C<T> a) { return mk<T>(a.x, -a.y); }
+// acc += a * b
+template <typename T> __host__ __device__ __forceinline__ void cfma(C<T> &acc, C<T> a, C<T> b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+// acc += conj(a) * b
+template <typename T> __host__ __device__ __forceinline__ void cfma_conj(C<T> &acc, C<T> a, C<T> b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(-a.y, b.x, acc.y);
+}
+// Complex division (Smith's algorithm, scaled to avoid overflow).
+template <typename T> __host__ __device__ __forceinline__ C<T> cdiv(C<T> a, C<T> b) {
+    T ar = b.x, ai = b.y;
+    if (fabs(ar) >= fabs(ai)) {
+        T r = ai / ar, d = ar + ai * r;
+        return mk<T>((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+    } else {
+        T r = ar / ai, d = ai + ar * r;
+        return mk<T>((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+    }
+}
+
+// ---------------------------------------------------------------- errors
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define EGX_CUDA(call)                                                                 \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess)                                                         \
+            throw ::egx::Error(EGX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define EGX_CHECK(cond, code, msg)                                                     \
+    do {                                                                               \
+        if (!(cond)) throw ::egx::Error((code), (msg));                                \
+    } while (0)
+
+// Device buffer owned by the context.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() {}
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void ensure(size_t n) {
+        if (n <= bytes) return;
+        release();
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw Error(EGX_ERR_OOM, "cudaMalloc of " + std::to_string(n) + " bytes failed: " + cudaGetErrorString(e));
+        }
+        bytes = n;
+    }
+    template <typename X> X *as() const { return reinterpret_cast<X *>(p); }
+};
+
+}  // namespace egx

@@ -1,0 +1,464 @@
+// Device vector kernels and the host-side GMRES driver (see egx_krylov.cuh).
+#include <cmath>
+
+#include "egx_krylov.cuh"
+
+namespace egx {
+
+constexpr int kThreads = 256;
+
+template <typename T> struct Acc { typedef T type; };
+
+__device__ __forceinline__ double2 warp_sum2(double2 v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum; result valid in thread 0.
+__device__ double2 block_sum2(double2 v) {
+    __shared__ double2 red[32];
+    v = warp_sum2(v);
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        int nw = (blockDim.x + 31) >> 5;
+        v = lane < nw ? red[lane] : make_double2(0, 0);
+        v = warp_sum2(v);
+    }
+    return v;
+}
+__device__ double block_sum(double v) {
+    __shared__ double red1[32];
+    v = warp_sum(v);
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red1[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        int nw = (blockDim.x + 31) >> 5;
+        v = lane < nw ? red1[lane] : 0.0;
+        v = warp_sum(v);
+    }
+    return v;
+}
+
+template <typename T>
+__global__ void k_multi_dot(const C<T> *__restrict__ V, int ncols, const C<T> *__restrict__ w, long n,
+                            double2 *__restrict__ partials) {
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (int k = 0; k < ncols; k++) {
+        const C<T> *col = V + (long)k * n;
+        C<T> acc = mk<T>(0, 0);
+        for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride)
+            cfma_conj<T>(acc, col[r], w[r]);
+        double2 s = block_sum2(make_double2((double)acc.x, (double)acc.y));
+        if (threadIdx.x == 0) partials[(long)blockIdx.x * ncols + k] = s;
+    }
+}
+
+__global__ void k_reduce_cols(const double2 *__restrict__ partials, int nblocks, int ncols, double2 *__restrict__ out) {
+    const int k = blockIdx.x;
+    double2 s = make_double2(0, 0);
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        double2 p = partials[(long)b * ncols + k];
+        s.x += p.x;
+        s.y += p.y;
+    }
+    s = block_sum2(s);
+    if (threadIdx.x == 0) out[k] = s;
+}
+
+__global__ void k_reduce_scalar(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
+    double s = 0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[b];
+    s = block_sum(s);
+    if (threadIdx.x == 0) out[0] = s;
+}
+
+template <typename T>
+__global__ void k_update_norm(const C<T> *__restrict__ V, int ncols, const double2 *__restrict__ dots, C<T> *w, long n,
+                              double *__restrict__ partials) {
+    __shared__ C<T> sd[64];
+    for (int k = threadIdx.x; k < ncols; k += blockDim.x) sd[k] = mk<T>((T)dots[k].x, (T)dots[k].y);
+    __syncthreads();
+    const long stride = (long)gridDim.x * blockDim.x;
+    T acc = 0;
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        C<T> v = w[r];
+        for (int k = 0; k < ncols; k++) {
+            C<T> a = V[(long)k * n + r];
+            C<T> d = sd[k];
+            // v -= a * d
+            v.x = fma(-a.x, d.x, v.x);
+            v.x = fma(a.y, d.y, v.x);
+            v.y = fma(-a.x, d.y, v.y);
+            v.y = fma(-a.y, d.x, v.y);
+        }
+        w[r] = v;
+        acc = fma(v.x, v.x, acc);
+        acc = fma(v.y, v.y, acc);
+    }
+    double s = block_sum((double)acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+template <typename T>
+__global__ void k_norm2(const C<T> *__restrict__ x, long n, double *__restrict__ partials) {
+    const long stride = (long)gridDim.x * blockDim.x;
+    T acc = 0;
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        C<T> v = x[r];
+        acc = fma(v.x, v.x, acc);
+        acc = fma(v.y, v.y, acc);
+    }
+    double s = block_sum((double)acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+template <typename T>
+__global__ void k_scale(const C<T> *__restrict__ x, T a, C<T> *__restrict__ y, long n) {
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+        y[r] = mk<T>(x[r].x * a, x[r].y * a);
+}
+template <typename T>
+__global__ void k_divide(const C<T> *__restrict__ x, T d, C<T> *__restrict__ y, long n) {
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+        y[r] = mk<T>(x[r].x / d, x[r].y / d);
+}
+template <typename T>
+__global__ void k_sub(const C<T> *__restrict__ a, const C<T> *__restrict__ b, C<T> *__restrict__ y, long n) {
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+        y[r] = csub<T>(a[r], b[r]);
+}
+template <typename T>
+__global__ void k_add(const C<T> *__restrict__ x, C<T> *__restrict__ y, long n) {
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+        y[r] = cadd<T>(y[r], x[r]);
+}
+template <typename T>
+__global__ void k_gemv(const C<T> *__restrict__ V, int ncols, const double2 *__restrict__ coef, C<T> *__restrict__ out,
+                       long n) {
+    __shared__ C<T> sc[64];
+    for (int k = threadIdx.x; k < ncols; k += blockDim.x) sc[k] = mk<T>((T)coef[k].x, (T)coef[k].y);
+    __syncthreads();
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+        C<T> acc = mk<T>(0, 0);
+        for (int k = 0; k < ncols; k++) cfma<T>(acc, V[(long)k * n + r], sc[k]);
+        out[r] = acc;
+    }
+}
+
+__global__ void k_d2f(const double2 *__restrict__ x, float2 *__restrict__ y, long n, double sc) {
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+        y[r] = make_float2((float)(x[r].x * sc), (float)(x[r].y * sc));
+}
+__global__ void k_f2d_add(const float2 *__restrict__ x, double2 *__restrict__ y, long n, double sc) {
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+        double2 v = y[r];
+        v.x += (double)x[r].x * sc;
+        v.y += (double)x[r].y * sc;
+        y[r] = v;
+    }
+}
+
+static int grid_for(long n) {
+    long g = (n + kThreads - 1) / kThreads;
+    if (g > 2048) g = 2048;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+template <typename T>
+void VecOps<T>::multi_dot(const C<T> *V, int ncols, const C<T> *w, long n, double2 *dots_dev, double2 *partials,
+                          int nblocks, cudaStream_t s) {
+    k_multi_dot<T><<<nblocks, kThreads, 0, s>>>(V, ncols, w, n, partials);
+    k_reduce_cols<<<ncols, kThreads, 0, s>>>(partials, nblocks, ncols, dots_dev);
+}
+template <typename T>
+void VecOps<T>::update_norm(const C<T> *V, int ncols, const double2 *dots_dev, C<T> *w, long n, double *norm2_dev,
+                            double *partials, int nblocks, cudaStream_t s) {
+    k_update_norm<T><<<nblocks, kThreads, 0, s>>>(V, ncols, dots_dev, w, n, partials);
+    k_reduce_scalar<<<1, kThreads, 0, s>>>(partials, nblocks, norm2_dev);
+}
+template <typename T>
+void VecOps<T>::norm2(const C<T> *x, long n, double *norm2_dev, double *partials, int nblocks, cudaStream_t s) {
+    k_norm2<T><<<nblocks, kThreads, 0, s>>>(x, n, partials);
+    k_reduce_scalar<<<1, kThreads, 0, s>>>(partials, nblocks, norm2_dev);
+}
+template <typename T>
+void VecOps<T>::scale(const C<T> *x, double a, C<T> *y, long n, cudaStream_t s) {
+    k_scale<T><<<grid_for(n), kThreads, 0, s>>>(x, (T)a, y, n);
+}
+template <typename T>
+void VecOps<T>::divide(const C<T> *x, double d, C<T> *y, long n, cudaStream_t s) {
+    k_divide<T><<<grid_for(n), kThreads, 0, s>>>(x, (T)d, y, n);
+}
+template <typename T>
+void VecOps<T>::sub(const C<T> *a, const C<T> *b, C<T> *y, long n, cudaStream_t s) {
+    k_sub<T><<<grid_for(n), kThreads, 0, s>>>(a, b, y, n);
+}
+template <typename T>
+void VecOps<T>::add(const C<T> *x, C<T> *y, long n, cudaStream_t s) {
+    k_add<T><<<grid_for(n), kThreads, 0, s>>>(x, y, n);
+}
+template <typename T>
+void VecOps<T>::gemv(const C<T> *V, int ncols, const double2 *coef, C<T> *out, long n, cudaStream_t s) {
+    k_gemv<T><<<grid_for(n), kThreads, 0, s>>>(V, ncols, coef, out, n);
+}
+template <typename T>
+void VecOps<T>::copy(const C<T> *x, C<T> *y, long n, cudaStream_t s) {
+    if (x != y) EGX_CUDA(cudaMemcpyAsync(y, x, n * sizeof(C<T>), cudaMemcpyDeviceToDevice, s));
+}
+template <typename T>
+void VecOps<T>::zero(C<T> *x, long n, cudaStream_t s) {
+    EGX_CUDA(cudaMemsetAsync(x, 0, n * sizeof(C<T>), s));
+}
+
+void convert_d2f(const double2 *x, float2 *y, long n, double scale, cudaStream_t s) {
+    k_d2f<<<grid_for(n), kThreads, 0, s>>>(x, y, n, scale);
+}
+void convert_f2d_add(const float2 *x, double2 *y, long n, double scale, cudaStream_t s) {
+    k_f2d_add<<<grid_for(n), kThreads, 0, s>>>(x, y, n, scale);
+}
+
+template struct VecOps<double>;
+template struct VecOps<float>;
+
+// ------------------------------------------------------------------ driver
+
+template <typename T>
+Gmres<T>::Gmres(long n, int m, double tol, int max_restarts, bool check_true, cudaStream_t s)
+    : n_(n), m_(m), tol_(tol), max_restarts_(max_restarts), check_true_(check_true), s_(s) {
+    EGX_CHECK(m >= 1 && m <= 60, EGX_ERR_INVALID, "GMRES buffer length must be in [1, 60]");
+    nblocks_ = grid_for(n);
+    if (nblocks_ > 1024) nblocks_ = 1024;
+    auto alloc = [](void **p, size_t b) {
+        cudaError_t e = cudaMalloc(p, b);
+        if (e != cudaSuccess) throw Error(EGX_ERR_OOM, std::string("GMRES workspace: ") + cudaGetErrorString(e));
+    };
+    alloc((void **)&V_, sizeof(C<T>) * n * m);
+    alloc((void **)&w_, sizeof(C<T>) * n);
+    alloc((void **)&r0_, sizeof(C<T>) * n);
+    alloc((void **)&xcur_, sizeof(C<T>) * n);
+    alloc((void **)&dots_, sizeof(double2) * 64 + sizeof(double) * 2);
+    norm_dev_ = reinterpret_cast<double *>(dots_ + 64);
+    alloc((void **)&coef_, sizeof(double2) * 64);
+    alloc((void **)&partials_, sizeof(double2) * (size_t)nblocks_ * 64);
+    EGX_CUDA(cudaMallocHost((void **)&host_, sizeof(double2) * 64 + sizeof(double) * 2));
+    H_.assign((size_t)(m + 1) * (m + 1), 0.0);
+    cs_.assign(m, 0.0);
+    sn_.assign(m, 0.0);
+}
+
+template <typename T>
+Gmres<T>::~Gmres() {
+    cudaFree(V_);
+    if (Z_) cudaFree(Z_);
+    cudaFree(w_);
+    cudaFree(r0_);
+    cudaFree(xcur_);
+    cudaFree(dots_);
+    cudaFree(coef_);
+    cudaFree(partials_);
+    cudaFreeHost(host_);
+}
+
+template <typename T>
+double Gmres<T>::norm(const C<T> *x) {
+    VecOps<T>::norm2(x, n_, norm_dev_, reinterpret_cast<double *>(partials_), nblocks_, s_);
+    kernel_launches += 2;
+    EGX_CUDA(cudaMemcpyAsync(host_, norm_dev_, sizeof(double), cudaMemcpyDeviceToHost, s_));
+    EGX_CUDA(cudaStreamSynchronize(s_));
+    return std::sqrt(host_[0]);
+}
+
+template <typename T>
+void Gmres<T>::construct(int jh, C<T> *result) {
+    // y = H(0:jh, 0:jh) \ g (SimplifiedZtrsv, upper, non-unit)
+    std::vector<std::complex<double>> y(jh > 0 ? jh : 1);
+    for (int i = 0; i < jh; i++) y[i] = h(i, m_);
+    for (int j = jh - 1; j >= 0; j--) {
+        if (y[j] != std::complex<double>(0.0, 0.0)) {
+            y[j] /= h(j, j);
+            std::complex<double> t = y[j];
+            for (int i = j - 1; i >= 0; i--) y[i] -= t * h(i, j);
+        }
+    }
+    if (jh > 0) {
+        EGX_CUDA(cudaMemcpyAsync(coef_, y.data(), sizeof(double2) * jh, cudaMemcpyHostToDevice, s_));
+        VecOps<T>::gemv(precond ? Z_ : V_, jh, coef_, r0_, n_, s_);
+        VecOps<T>::add(r0_, result, n_, s_);
+        kernel_launches += 2;
+        // the host vector y must outlive the async copy
+        EGX_CUDA(cudaStreamSynchronize(s_));
+    }
+}
+
+template <typename T>
+double Gmres<T>::final_actions(int jh, const C<T> *rhs, C<T> *result) {
+    construct(jh, result);
+    if (!check_true_) return -1.0;
+    VecOps<T>::copy(result, r0_, n_, s_);
+    apply(r0_, w_);
+    VecOps<T>::sub(rhs, w_, w_, n_, s_);
+    kernel_launches += 1;
+    double tn = norm(w_);
+    return tn / bn_;
+}
+
+template <typename T>
+double Gmres<T>::arnoldi(double bn, int &jh) {
+    double bea = -1.0;
+    const int m = m_;
+    do {
+        C<T> *vj = V_ + (long)jh * n_;
+        if (precond) {
+            C<T> *zj = Z_ + (long)jh * n_;
+            precond(vj, zj);
+            VecOps<T>::copy(zj, w_, n_, s_);
+        } else {
+            VecOps<T>::copy(vj, w_, n_, s_);
+        }
+        apply(w_, r0_);
+        VecOps<T>::copy(r0_, w_, n_, s_);
+        for (int j = 0; j <= jh; j++) h(j, jh) = 0.0;
+        int northo = 0;
+        double dloo = 0, dnormw = 0;
+        do {
+            northo++;
+            VecOps<T>::multi_dot(V_, jh + 1, w_, n_, dots_, partials_, nblocks_, s_);
+            VecOps<T>::update_norm(V_, jh + 1, dots_, w_, n_, norm_dev_, reinterpret_cast<double *>(partials_),
+                                   nblocks_, s_);
+            kernel_launches += 4;
+            EGX_CUDA(cudaMemcpyAsync(host_, dots_, sizeof(double2) * 64 + sizeof(double), cudaMemcpyDeviceToHost, s_));
+            EGX_CUDA(cudaStreamSynchronize(s_));
+            const double2 *hd = reinterpret_cast<const double2 *>(host_);
+            double ss = 0;
+            for (int j = 0; j <= jh; j++) {
+                h(j, jh) += std::complex<double>(hd[j].x, hd[j].y);
+                ss += hd[j].x * hd[j].x + hd[j].y * hd[j].y;
+            }
+            dloo = ss;
+            dnormw = std::sqrt(host_[2 * 64]);
+        } while (2.0 * dnormw <= std::sqrt(dloo) && northo < 3);
+        h(jh + 1, jh) = dnormw;
+        if (jh < m - 1) {
+            VecOps<T>::divide(w_, dnormw, V_ + (long)(jh + 1) * n_, n_, s_);
+            kernel_launches += 1;
+        }
+        auto rot = [](std::complex<double> &x, std::complex<double> &y, double c, std::complex<double> s) {
+            std::complex<double> t = c * x + s * y;
+            y = c * y - std::conj(s) * x;
+            x = t;
+        };
+        for (int j = 0; j < jh; j++) rot(h(j, jh), h(j + 1, jh), cs_[j], sn_[j]);
+        // zrotg (classic reference algorithm)
+        {
+            std::complex<double> a = h(jh, jh), b = h(jh + 1, jh);
+            double c;
+            std::complex<double> s;
+            if (std::abs(a) == 0.0) {
+                c = 0.0;
+                s = 1.0;
+            } else {
+                double scale = std::abs(a) + std::abs(b);
+                double a1 = std::abs(a / scale), b1 = std::abs(b / scale);
+                double nrm = scale * std::sqrt(a1 * a1 + b1 * b1);
+                std::complex<double> alpha = a / std::abs(a);
+                c = std::abs(a) / nrm;
+                s = alpha * std::conj(b) / nrm;
+            }
+            cs_[jh] = c;
+            sn_[jh] = s;
+        }
+        rot(h(jh, m), h(jh + 1, m), cs_[jh], sn_[jh]);
+        rot(h(jh, jh), h(jh + 1, jh), cs_[jh], sn_[jh]);
+        h(jh + 1, jh) = 0.0;
+        double dnormres = std::abs(h(jh + 1, m));
+        bea = dnormres / bn;
+        iterations_done_++;
+        if (on_iteration) on_iteration(iterations_done_, bea);
+        jh++;
+    } while (bea > tol_ && jh < m);
+    return bea;
+}
+
+template <typename T>
+GmresResult Gmres<T>::solve(const C<T> *rhs, const C<T> *x0, C<T> *result) {
+    GmresResult res;
+    iterations_done_ = 0;
+    if (precond && !Z_) {
+        cudaError_t e = cudaMalloc((void **)&Z_, sizeof(C<T>) * n_ * m_);
+        if (e != cudaSuccess) throw Error(EGX_ERR_OOM, "FGMRES preconditioned basis allocation failed");
+    }
+    double bn = norm(rhs);
+    bn_ = bn;
+    if (bn == 0) {
+        res.converged = true;
+        res.arnoldi_be = 0;
+        res.true_be = 0;
+        return res;
+    }
+    apply(x0, r0_);
+    VecOps<T>::sub(rhs, r0_, r0_, n_, s_);
+    VecOps<T>::copy(r0_, w_, n_, s_);
+    kernel_launches += 1;
+    double beta = norm(w_);
+    if (beta == 0) {
+        VecOps<T>::copy(x0, result, n_, s_);
+        res.converged = true;
+        res.arnoldi_be = 0;
+        res.true_be = 0;
+        res.iterations = 1;
+        return res;
+    }
+    double bea = -1, be = -1;
+    int iter = 0;
+    VecOps<T>::copy(x0, result, n_, s_);
+    while (true) {
+        VecOps<T>::scale(w_, 1.0 / beta, V_, n_, s_);
+        kernel_launches += 1;
+        h(0, m_) = beta;
+        for (int i = 1; i <= m_; i++) h(i, m_) = 0.0;
+        int jh = 0;
+        bea = arnoldi(bn, jh);
+        if (bea < tol_) {
+            be = final_actions(jh, rhs, result);
+            res.converged = true;
+            res.arnoldi_be = bea;
+            res.true_be = be;
+            res.iterations = iterations_done_;
+            return res;
+        }
+        iter++;
+        if (iter >= max_restarts_) break;
+        // PrepareRestart with the true residual
+        construct(jh, result);
+        VecOps<T>::copy(result, w_, n_, s_);
+        apply(w_, r0_);
+        VecOps<T>::sub(rhs, r0_, r0_, n_, s_);
+        VecOps<T>::copy(r0_, w_, n_, s_);
+        kernel_launches += 1;
+        beta = norm(w_);
+    }
+    be = final_actions(m_, rhs, result);
+    res.converged = false;
+    res.arnoldi_be = bea;
+    res.true_be = be;
+    res.iterations = iterations_done_;
+    return res;
+}
+
+template class Gmres<double>;
+template class Gmres<float>;
+
+}  // namespace egx

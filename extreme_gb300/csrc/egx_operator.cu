@@ -1,0 +1,311 @@
+// CIE convolution operator kernels.
+//
+// One apply (ConvolutionOperator.CalculateOperatorAorKr, ConvolutionOperator.cs:162-171)
+// is five kernels over the spectral buffer buf[2nx][2ny][B], B = nrhs*3*nz:
+//   k_fwd_y     : rx = r*x, scale by the forward factors, zero-pad, DFT along y
+//                 (ApplyOperatorR + PrepareForForwardFft + half of the forward FFT);
+//                 only the nx rows that hold data are transformed;
+//   k_lines     : DFT along x over all 2ny columns, reading only the nx non-zero rows;
+//   k_contract  : per spectral point, the 3x3 block product with the Green tensor
+//                 (ApplyGreenTensorAlongZ, :274-327), one CTA per stored quadrant point
+//                 serving the up to four points that share its block;
+//   k_lines     : inverse DFT along x, writing only the nx rows that are extracted;
+//   k_bwd_y     : inverse DFT along y, extraction with the backward factors and the
+//                 last step (ExtractData + PerformLastStep, :187-231).
+#include "egx_operator.cuh"
+
+namespace egx {
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ int sym_index(int i, int j) {
+    return (i <= j) ? i + j * (j + 1) / 2 : j + i * (i + 1) / 2;
+}
+
+template <typename T>
+__global__ void k_fwd_y(const C<T> *__restrict__ x, const OperatorData<T> op, C<T> *__restrict__ buf, const OpDims d,
+                        const FftPlan plan, const C<T> *__restrict__ tw, int bt) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C<T> *sa = reinterpret_cast<C<T> *>(smem_raw);
+    C<T> *sb = sa + plan.n * bt;
+    const int i = blockIdx.x;
+    const int b0 = blockIdx.y * bt;
+    const int n1 = plan.n;
+    const int per = 3 * d.nz;
+    for (int item = threadIdx.x; item < n1 * bt; item += blockDim.x) {
+        int j = item / bt, col = item - j * bt;
+        int b = b0 + col;
+        C<T> v = mk<T>(0, 0);
+        if (j < d.ny && b < d.B) {
+            int rhs = b / per, rem = b - rhs * per;
+            int k = rem % d.nz, c = rem / d.nz;
+            long cell = (long)i * d.ny + j;
+            C<T> xv = x[rhs * d.nvec + (cell * 3 + c) * d.nz + k];
+            C<T> rx = cmul<T>(op.r[cell * d.nz + k], xv);
+            v = cmul<T>(op.fwd[k], rx);
+        }
+        sa[item] = v;
+    }
+    __syncthreads();
+    C<T> *res = fft_smem<T>(sa, sb, plan, bt, tw, -1);
+    for (int item = threadIdx.x; item < n1 * bt; item += blockDim.x) {
+        int j = item / bt, col = item - j * bt;
+        int b = b0 + col;
+        if (b < d.B) buf[((long)i * n1 + j) * d.B + b] = res[item];
+    }
+}
+
+// DFT of `lines` interleaved sequences: element e of line L, column b at
+// base + L*lstride + e*estride + b. Elements e >= nload read as zero, only
+// e < nstore are written back.
+template <typename T>
+__global__ void k_lines(C<T> *buf, long lstride, long estride, int B, int nload, int nstore, const FftPlan plan,
+                        const C<T> *__restrict__ tw, int bt, int sign) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C<T> *sa = reinterpret_cast<C<T> *>(smem_raw);
+    C<T> *sb = sa + plan.n * bt;
+    const long base = (long)blockIdx.x * lstride;
+    const int b0 = blockIdx.y * bt;
+    const int n = plan.n;
+    for (int item = threadIdx.x; item < n * bt; item += blockDim.x) {
+        int e = item / bt, col = item - e * bt;
+        int b = b0 + col;
+        C<T> v = mk<T>(0, 0);
+        if (e < nload && b < B) v = buf[base + e * estride + b];
+        sa[item] = v;
+    }
+    __syncthreads();
+    C<T> *res = fft_smem<T>(sa, sb, plan, bt, tw, sign);
+    for (int item = threadIdx.x; item < n * bt; item += blockDim.x) {
+        int e = item / bt, col = item - e * bt;
+        int b = b0 + col;
+        if (e < nstore && b < B) buf[base + e * estride + b] = res[item];
+    }
+}
+
+template <typename T>
+__global__ void k_bwd_y(const C<T> *__restrict__ buf, const C<T> *__restrict__ x, const OperatorData<T> op,
+                        C<T> *__restrict__ y, const OpDims d, const FftPlan plan, const C<T> *__restrict__ tw, int bt) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C<T> *sa = reinterpret_cast<C<T> *>(smem_raw);
+    C<T> *sb = sa + plan.n * bt;
+    const int i = blockIdx.x;
+    const int b0 = blockIdx.y * bt;
+    const int n1 = plan.n;
+    const int per = 3 * d.nz;
+    for (int item = threadIdx.x; item < n1 * bt; item += blockDim.x) {
+        int j = item / bt, col = item - j * bt;
+        int b = b0 + col;
+        sa[item] = (b < d.B) ? buf[((long)i * n1 + j) * d.B + b] : mk<T>(0, 0);
+    }
+    __syncthreads();
+    C<T> *res = fft_smem<T>(sa, sb, plan, bt, tw, +1);
+    for (int item = threadIdx.x; item < d.ny * bt; item += blockDim.x) {
+        int j = item / bt, col = item - j * bt;
+        int b = b0 + col;
+        if (b >= d.B) continue;
+        int rhs = b / per, rem = b - rhs * per;
+        int k = rem % d.nz, c = rem / d.nz;
+        long cell = (long)i * d.ny + j;
+        long idx = rhs * d.nvec + (cell * 3 + c) * d.nz + k;
+        C<T> yv = cmul<T>(op.bwd[k], res[item]);
+        C<T> xv = x[idx];
+        C<T> rx = cmul<T>(op.r[cell * d.nz + k], xv);
+        C<T> out;
+        if (op.type == EGX_OP_A) out = csub<T>(csub<T>(xv, yv), rx);
+        else out = cadd<T>(yv, rx);
+        y[idx] = out;
+    }
+}
+
+// Block contraction, one CTA per stored quadrant point (a, b). The block is
+// staged in shared memory when it fits (G_IN_SMEM), else read through L1.
+template <typename T, bool G_IN_SMEM>
+__global__ void k_contract(C<T> *buf, const C<T> *__restrict__ G, const OpDims d) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nz = d.nz;
+    const int S = nz * (nz + 1) / 2, A = nz * nz, Bs = 4 * S + 2 * A;
+    const int q = blockIdx.x;
+    const int a = q / (d.ny + 1), bq = q - a * (d.ny + 1);
+    const int n1 = 2 * d.ny;
+    const int kx[2] = {a, 2 * d.nx - a};
+    const int ky[2] = {bq, 2 * d.ny - bq};
+    const int nkx = (a == 0 || a == d.nx) ? 1 : 2;
+    const int nky = (bq == 0 || bq == d.ny) ? 1 : 2;
+    const int npts = nkx * nky;
+    const int per = 3 * nz;
+    const int nv = npts * d.nrhs;
+
+    C<T> *sX = reinterpret_cast<C<T> *>(smem_raw);
+    C<T> *sG = sX + 4 * d.nrhs * per;
+    const C<T> *gq = G + (long)q * Bs;
+    const C<T> *g;
+    if (G_IN_SMEM) {
+        for (int t = threadIdx.x; t < Bs; t += blockDim.x) sG[t] = gq[t];
+        g = sG;
+    } else {
+        g = gq;
+    }
+    for (int t = threadIdx.x; t < nv * per; t += blockDim.x) {
+        int v = t / per, e = t - v * per;
+        int p = v / d.nrhs, rhs = v - p * d.nrhs;
+        long pt = (long)kx[p / nky] * n1 + ky[p % nky];
+        sX[t] = buf[pt * d.B + rhs * per + e];
+    }
+    __syncthreads();
+    const C<T> *gxx = g, *gxy = g + S, *gyy = g + 2 * S, *gzz = g + 3 * S;
+    const C<T> *gxz = g + 4 * S, *gyz = g + 4 * S + A;
+    for (int o = threadIdx.x; o < per * nv; o += blockDim.x) {
+        int v = o % nv;
+        int ci = o / nv;
+        int cout = ci / nz, i = ci - cout * nz;
+        int p = v / d.nrhs, rhs = v - p * d.nrhs;
+        int mx = (p / nky) == 1, my = (p % nky) == 1;
+        const C<T> *X = sX + v * per;
+        C<T> a1 = mk<T>(0, 0), a2 = mk<T>(0, 0), a3 = mk<T>(0, 0);
+        if (cout == 0) {
+            for (int j = 0; j < nz; j++) {
+                int s = sym_index(i, j);
+                cfma<T>(a1, gxx[s], X[j]);
+                cfma<T>(a2, gxy[s], X[nz + j]);
+                cfma<T>(a3, gxz[i * nz + j], X[2 * nz + j]);
+            }
+            // Sxy odd/odd, Axz odd in x
+            if (mx != my) a2 = mk<T>(-a2.x, -a2.y);
+            if (mx) a3 = mk<T>(-a3.x, -a3.y);
+        } else if (cout == 1) {
+            for (int j = 0; j < nz; j++) {
+                int s = sym_index(i, j);
+                cfma<T>(a1, gxy[s], X[j]);
+                cfma<T>(a2, gyy[s], X[nz + j]);
+                cfma<T>(a3, gyz[i * nz + j], X[2 * nz + j]);
+            }
+            if (mx != my) a1 = mk<T>(-a1.x, -a1.y);
+            if (my) a3 = mk<T>(-a3.x, -a3.y);
+        } else {
+            for (int j = 0; j < nz; j++) {
+                cfma<T>(a1, gxz[j * nz + i], X[j]);
+                cfma<T>(a2, gyz[j * nz + i], X[nz + j]);
+                cfma<T>(a3, gzz[sym_index(i, j)], X[2 * nz + j]);
+            }
+            // -Axz^T x - Ayz^T y
+            if (!mx) a1 = mk<T>(-a1.x, -a1.y);
+            if (!my) a2 = mk<T>(-a2.x, -a2.y);
+        }
+        C<T> acc = cadd<T>(cadd<T>(a1, a2), a3);
+        long pt = (long)kx[p / nky] * n1 + ky[p % nky];
+        buf[pt * d.B + rhs * per + cout * nz + i] = acc;
+    }
+}
+
+static int threads_for(int items) { return items >= 256 ? 256 : (items >= 128 ? 128 : 64); }
+
+template <typename T>
+static void set_smem(const void *fn, size_t bytes) {
+    if (bytes > 48 * 1024) EGX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
+template <typename T>
+void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, const C<T> *x, C<T> *y, C<T> *buf,
+                    const C<T> *tw0, const C<T> *tw1, const FftPlan &p0, const FftPlan &p1, cudaStream_t s,
+                    long *launches) {
+    const int n0 = 2 * d.nx, n1 = 2 * d.ny;
+    // 1. r*x, forward factors, zero padding, DFT along y (rows i < nx)
+    {
+        int bt = fft_cols(n1, sizeof(C<T>));
+        size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
+        set_smem<T>((const void *)k_fwd_y<T>, sm);
+        dim3 grid(d.nx, (d.B + bt - 1) / bt);
+        k_fwd_y<T><<<grid, threads_for(n1 * bt / 2), sm, s>>>(x, op, buf, d, p1, tw1, bt);
+    }
+    // 2. DFT along x over all columns; rows >= nx are zero
+    {
+        int bt = fft_cols(n0, sizeof(C<T>));
+        size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
+        set_smem<T>((const void *)k_lines<T>, sm);
+        dim3 grid(n1, (d.B + bt - 1) / bt);
+        k_lines<T><<<grid, threads_for(n0 * bt / 2), sm, s>>>(buf, d.B, (long)n1 * d.B, d.B, d.nx, n0, p0, tw0, bt,
+                                                              -1);
+    }
+    // 3. block contraction
+    {
+        GreenDims gd{d.nx, d.ny, d.nz};
+        size_t sx = (size_t)4 * d.nrhs * 3 * d.nz * sizeof(C<T>);
+        size_t sg = (size_t)gd.Bs() * sizeof(C<T>);
+        int thr = 256;
+        if (sx + sg <= 200 * 1024) {
+            set_smem<T>((const void *)k_contract<T, true>, sx + sg);
+            k_contract<T, true><<<(unsigned)gd.Q(), thr, sx + sg, s>>>(buf, G, d);
+        } else {
+            set_smem<T>((const void *)k_contract<T, false>, sx);
+            k_contract<T, false><<<(unsigned)gd.Q(), thr, sx, s>>>(buf, G, d);
+        }
+    }
+    // 4. inverse DFT along x; only rows < nx are needed afterwards
+    {
+        int bt = fft_cols(n0, sizeof(C<T>));
+        size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
+        dim3 grid(n1, (d.B + bt - 1) / bt);
+        k_lines<T><<<grid, threads_for(n0 * bt / 2), sm, s>>>(buf, d.B, (long)n1 * d.B, d.B, n0, d.nx, p0, tw0, bt,
+                                                              +1);
+    }
+    // 5. inverse DFT along y, extraction, last step
+    {
+        int bt = fft_cols(n1, sizeof(C<T>));
+        size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
+        set_smem<T>((const void *)k_bwd_y<T>, sm);
+        dim3 grid(d.nx, (d.B + bt - 1) / bt);
+        k_bwd_y<T><<<grid, threads_for(n1 * bt / 2), sm, s>>>(buf, x, op, y, d, p1, tw1, bt);
+    }
+    EGX_CUDA(cudaGetLastError());
+    if (launches) *launches += 5;
+}
+
+template <typename T>
+void fft2d(C<T> *buf, int n0, int n1, int howmany, int sign, const C<T> *tw0, const C<T> *tw1, const FftPlan &p0,
+           const FftPlan &p1, cudaStream_t s, long *launches) {
+    {
+        int bt = fft_cols(n1, sizeof(C<T>));
+        size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
+        set_smem<T>((const void *)k_lines<T>, sm);
+        dim3 grid(n0, (howmany + bt - 1) / bt);
+        k_lines<T><<<grid, threads_for(n1 * bt / 2), sm, s>>>(buf, (long)n1 * howmany, howmany, howmany, n1, n1, p1,
+                                                              tw1, bt, sign);
+    }
+    {
+        int bt = fft_cols(n0, sizeof(C<T>));
+        size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
+        set_smem<T>((const void *)k_lines<T>, sm);
+        dim3 grid(n1, (howmany + bt - 1) / bt);
+        k_lines<T><<<grid, threads_for(n0 * bt / 2), sm, s>>>(buf, howmany, (long)n1 * howmany, howmany, n0, n0, p0,
+                                                              tw0, bt, sign);
+    }
+    EGX_CUDA(cudaGetLastError());
+    if (launches) *launches += 2;
+}
+
+std::vector<double> twiddles(int n) {
+    std::vector<double> t(2 * (size_t)n);
+    for (int m = 0; m < n; m++) {
+        // reduce to the first octant for accuracy
+        double ang = 2.0 * M_PI * (double)m / (double)n;
+        t[2 * m] = cos(ang);
+        t[2 * m + 1] = -sin(ang);
+        if (4 * m == n) { t[2 * m] = 0.0; t[2 * m + 1] = -1.0; }
+        if (2 * m == n) { t[2 * m] = -1.0; t[2 * m + 1] = 0.0; }
+        if (4 * m == 3 * n) { t[2 * m] = 0.0; t[2 * m + 1] = 1.0; }
+    }
+    return t;
+}
+
+template void operator_apply<double>(const OpDims &, const OperatorData<double> &, const C<double> *,
+                                     const C<double> *, C<double> *, C<double> *, const C<double> *,
+                                     const C<double> *, const FftPlan &, const FftPlan &, cudaStream_t, long *);
+template void operator_apply<float>(const OpDims &, const OperatorData<float> &, const C<float> *, const C<float> *,
+                                    C<float> *, C<float> *, const C<float> *, const C<float> *, const FftPlan &,
+                                    const FftPlan &, cudaStream_t, long *);
+template void fft2d<double>(C<double> *, int, int, int, int, const C<double> *, const C<double> *, const FftPlan &,
+                            const FftPlan &, cudaStream_t, long *);
+template void fft2d<float>(C<float> *, int, int, int, int, const C<float> *, const C<float> *, const FftPlan &,
+                           const FftPlan &, cudaStream_t, long *);
+
+}  // namespace egx

@@ -1,0 +1,49 @@
+// The CIE convolution operator on the device
+// (Extreme.Cartesian/Forward/AtoA/ConvolutionOperator.cs:45-327).
+#pragma once
+
+#include "egx_fft.cuh"
+
+namespace egx {
+
+// Device-side spectral Green tensor: only the (nx+1) x (ny+1) quadrant of
+// spectral points is stored; the other three quadrants follow from the
+// parity of each component in real space (GreenTensorFftPopulator.cs:170-185):
+// xx, yy, zz even/even, xy odd/odd, xz odd in x, yz odd in y.
+// Per point, one contiguous block of Bs entries:
+//   xx | xy | yy | zz  (packed rc + tr*(tr+1)/2, S = nz(nz+1)/2 each)
+//   xz | yz            (rc*nz + tr, A = nz*nz each)
+struct GreenDims {
+    int nx, ny, nz;
+    int S() const { return nz * (nz + 1) / 2; }
+    int A() const { return nz * nz; }
+    int Bs() const { return 4 * S() + 2 * A(); }
+    long Q() const { return (long)(nx + 1) * (ny + 1); }
+};
+
+struct OpDims {
+    int nx, ny, nz, nrhs;
+    int B;       // batch of the spectral buffer: nrhs * 3 * nz
+    long nvec;   // elements of one anomaly vector: nx*ny*3*nz
+};
+
+template <typename T>
+struct OperatorData {
+    const C<T> *r;    // [nx*ny*nz]
+    const C<T> *fwd;  // [nz]
+    const C<T> *bwd;  // [nz]
+    int type;         // EGX_OP_A / EGX_OP_CHI0
+};
+
+// Launch the full apply y = K x (nrhs vectors) on `stream`.
+template <typename T>
+void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, const C<T> *x, C<T> *y, C<T> *buf,
+                    const C<T> *tw0, const C<T> *tw1, const FftPlan &p0, const FftPlan &p1, cudaStream_t s,
+                    long *launches);
+
+// In-place batched 2-D DFT (egx_fft2d).
+template <typename T>
+void fft2d(C<T> *buf, int n0, int n1, int howmany, int sign, const C<T> *tw0, const C<T> *tw1, const FftPlan &p0,
+           const FftPlan &p1, cudaStream_t s, long *launches);
+
+}  // namespace egx

@@ -1,0 +1,293 @@
+"""ctypes binding of ``libegx.so`` (the C ABI declared in ``include/egx.h``).
+
+This is the Python face of the drop-in boundary: the same entry points a C#
+P/Invoke layer binds. The library must be built
+(``python -m extreme_gb300._build``); there is no fallback when it is missing.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libegx.so")
+
+OK = 0
+ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_NOT_CONVERGED, ERR_TIMEOUT, ERR_STATE, ERR_MODEL = range(1, 8)
+OP_A, OP_CHI0 = 0, 1
+HOST, DEVICE = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+PRECOND_GMRES, PRECOND_CALLBACK, PRECOND_NONE = 0, 1, 2
+
+# Every symbol the header declares (checked by the ABI test).
+EXPORTS = [
+    "egx_create", "egx_destroy", "egx_last_error", "egx_version", "egx_set_stream", "egx_launch_count",
+    "egx_green_build", "egx_green_upload", "egx_green_download", "egx_green_free",
+    "egx_op_prepare", "egx_op_apply", "egx_op_apply_c64", "egx_fft2d",
+    "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond",
+]
+
+
+class EgxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("egx error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Model(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("dx", C.c_double), ("dy", C.c_double),
+                ("layer_depth", C.POINTER(C.c_double)), ("layer_thickness", C.POINTER(C.c_double)),
+                ("n_bg", C.c_int), ("zero_air_level", C.c_double),
+                ("bg_thickness", C.POINTER(C.c_double)), ("bg_sigma", C.POINTER(C.c_double))]
+
+
+class GmresParams(C.Structure):
+    _fields_ = [("m_out", C.c_int), ("m_in", C.c_int), ("tol", C.c_double), ("max_restarts", C.c_int),
+                ("precond", C.c_int), ("check_true", C.c_int)]
+
+
+class MixedParams(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_outer", C.c_int), ("m_out", C.c_int), ("m_in", C.c_int),
+                ("inner_tol", C.c_double), ("inner_restarts", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("converged", C.c_int), ("iterations", C.c_int), ("arnoldi_be", C.c_double),
+                ("true_be", C.c_double), ("n_applies", C.c_int), ("n_refinements", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+PRECOND_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_int)
+
+_lib = None
+
+
+def load(path=None):
+    """Load libegx.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError("libegx.so is not built (%s); run `python -m extreme_gb300._build`" % path)
+    lib = C.CDLL(path)
+    vp, i, d = C.c_void_p, C.c_int, C.c_double
+    lib.egx_create.argtypes = [i, C.POINTER(vp)]
+    lib.egx_destroy.argtypes = [vp]
+    lib.egx_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+    lib.egx_set_stream.argtypes = [vp, vp]
+    lib.egx_launch_count.argtypes = [vp]
+    lib.egx_launch_count.restype = C.c_long
+    lib.egx_green_build.argtypes = [vp, C.POINTER(Model), d, i, i, C.POINTER(vp)]
+    lib.egx_green_upload.argtypes = [vp, i, i, i, C.POINTER(vp), i, C.POINTER(vp)]
+    lib.egx_green_download.argtypes = [vp, vp, C.POINTER(vp)]
+    lib.egx_green_free.argtypes = [vp, vp]
+    lib.egx_op_prepare.argtypes = [vp, vp, vp, vp, vp, i]
+    lib.egx_op_apply.argtypes = [vp, vp, vp, i, i]
+    lib.egx_op_apply_c64.argtypes = [vp, vp, vp, i, i]
+    lib.egx_fft2d.argtypes = [vp, vp, i, i, i, i, i]
+    lib.egx_fgmres_solve.argtypes = [vp, vp, vp, C.POINTER(GmresParams), C.POINTER(Result), i]
+    lib.egx_mixed_solve.argtypes = [vp, vp, vp, C.POINTER(MixedParams), C.POINTER(Result), i]
+    lib.egx_set_precond.argtypes = [vp, i, PRECOND_FN, vp]
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+def _c128(a):
+    a = np.ascontiguousarray(a, np.complex128)
+    return a
+
+
+GREEN_COMPONENTS = ("xx", "xy", "yy", "zz", "xz", "yz")
+
+
+class Context:
+    """An ``egx_ctx``: one device, one stream."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = C.c_void_p()
+        self._check(self.lib.egx_create(device, C.byref(h)), None)
+        self.h = h
+        self._cb = None
+
+    def _check(self, rc, h="self"):
+        if rc != OK:
+            msg = ""
+            hh = self.h if h == "self" else h
+            if hh is not None:
+                buf = C.create_string_buffer(1024)
+                self.lib.egx_last_error(hh, buf, 1024)
+                msg = buf.value.decode()
+            raise EgxError(rc, msg)
+
+    def close(self):
+        if getattr(self, "h", None) is not None:
+            self.lib.egx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def launch_count(self):
+        return int(self.lib.egx_launch_count(self.h))
+
+    def set_stream(self, stream_handle):
+        self._check(self.lib.egx_set_stream(self.h, C.c_void_p(stream_handle)))
+
+    # -- Green tensor -----------------------------------------------------
+    def green_upload(self, G, nx, ny, nz, precision=PREC_FP64):
+        """G: dict c -> [2nx, 2ny, block] complex128 in the reference layout."""
+        arrs = [_c128(G[c]) for c in GREEN_COMPONENTS]
+        ptrs = (C.c_void_p * 6)(*[a.ctypes.data for a in arrs])
+        h = C.c_void_p()
+        self._check(self.lib.egx_green_upload(self.h, nx, ny, nz, ptrs, precision, C.byref(h)))
+        return GreenTensor(self, h, nx, ny, nz)
+
+    def green_build(self, model, omega, n_hankels=10, precision=PREC_FP64):
+        m = model_struct(model)
+        h = C.c_void_p()
+        self._check(self.lib.egx_green_build(self.h, C.byref(m.s), float(omega), int(n_hankels), precision,
+                                             C.byref(h)))
+        return GreenTensor(self, h, model.nx, model.ny, model.nz)
+
+    # -- operator ---------------------------------------------------------
+    def op_prepare(self, green, zeta, zeta0, dz, op_type):
+        z = _c128(zeta)
+        z0 = _c128(zeta0)
+        dz = np.ascontiguousarray(dz, np.float64)
+        self._check(self.lib.egx_op_prepare(self.h, green.h, _ptr(z), _ptr(z0), _ptr(dz), op_type))
+
+    def op_apply(self, x, nrhs=1, out=None):
+        """Host arrays (complex128)."""
+        x = _c128(x)
+        y = np.empty_like(x) if out is None else out
+        self._check(self.lib.egx_op_apply(self.h, _ptr(x), _ptr(y), nrhs, HOST))
+        return y
+
+    def op_apply_dev(self, x_ptr, y_ptr, nrhs=1):
+        self._check(self.lib.egx_op_apply(self.h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), nrhs, DEVICE))
+
+    def op_apply_c64(self, x, nrhs=1):
+        x = np.ascontiguousarray(x, np.complex64)
+        y = np.empty_like(x)
+        self._check(self.lib.egx_op_apply_c64(self.h, _ptr(x), _ptr(y), nrhs, HOST))
+        return y
+
+    def fft2d(self, buf, sign):
+        """In-place on a host array [n0, n1, howmany] complex128."""
+        assert buf.dtype == np.complex128 and buf.flags.c_contiguous and buf.ndim == 3
+        n0, n1, hm = buf.shape
+        self._check(self.lib.egx_fft2d(self.h, _ptr(buf), n0, n1, hm, sign, HOST))
+        return buf
+
+    # -- solver -----------------------------------------------------------
+    def fgmres_solve(self, b, x0, m_out=20, m_in=10, tol=1e-8, max_restarts=100, precond=PRECOND_GMRES,
+                     check_true=True, raise_on_nonconv=False):
+        b = _c128(b)
+        x = _c128(x0).copy()
+        p = GmresParams(m_out, m_in, tol, max_restarts, precond, int(check_true))
+        r = Result()
+        rc = self.lib.egx_fgmres_solve(self.h, _ptr(b), _ptr(x), C.byref(p), C.byref(r), HOST)
+        if rc != OK and not (rc == ERR_NOT_CONVERGED and not raise_on_nonconv):
+            self._check(rc)
+        return x, r.as_dict()
+
+    def fgmres_solve_dev(self, b_ptr, x_ptr, m_out=20, m_in=10, tol=1e-8, max_restarts=100,
+                         precond=PRECOND_GMRES, check_true=True):
+        p = GmresParams(m_out, m_in, tol, max_restarts, precond, int(check_true))
+        r = Result()
+        rc = self.lib.egx_fgmres_solve(self.h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(p), C.byref(r), DEVICE)
+        if rc not in (OK, ERR_NOT_CONVERGED):
+            self._check(rc)
+        return r.as_dict()
+
+    def mixed_solve(self, b, x0, tol=1e-6, max_outer=10, m_out=30, m_in=10, inner_tol=1e-4, inner_restarts=20):
+        b = _c128(b)
+        x = _c128(x0).copy()
+        p = MixedParams(tol, max_outer, m_out, m_in, inner_tol, inner_restarts)
+        r = Result()
+        rc = self.lib.egx_mixed_solve(self.h, _ptr(b), _ptr(x), C.byref(p), C.byref(r), HOST)
+        if rc not in (OK, ERR_NOT_CONVERGED):
+            self._check(rc)
+        return x, r.as_dict()
+
+    def mixed_solve_dev(self, b_ptr, x_ptr, tol=1e-6, max_outer=10, m_out=30, m_in=10, inner_tol=1e-4,
+                        inner_restarts=20):
+        p = MixedParams(tol, max_outer, m_out, m_in, inner_tol, inner_restarts)
+        r = Result()
+        rc = self.lib.egx_mixed_solve(self.h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(p), C.byref(r), DEVICE)
+        if rc not in (OK, ERR_NOT_CONVERGED):
+            self._check(rc)
+        return r.as_dict()
+
+    def set_precond(self, kind, fn=None):
+        """fn(src_ptr, dst_ptr, n, precision) -> None, device pointers."""
+        if kind == PRECOND_CALLBACK:
+            def tramp(user, src, dst, n, prec):
+                try:
+                    fn(src, dst, n, prec)
+                    return 0
+                except Exception:
+                    return 1
+            self._cb = PRECOND_FN(tramp)
+            self._check(self.lib.egx_set_precond(self.h, kind, self._cb, None))
+        else:
+            self._cb = None
+            self._check(self.lib.egx_set_precond(self.h, kind, PRECOND_FN(), None))
+
+
+class GreenTensor:
+    def __init__(self, ctx, h, nx, ny, nz):
+        self.ctx, self.h, self.nx, self.ny, self.nz = ctx, h, nx, ny, nz
+
+    def download(self):
+        nx, ny, nz = self.nx, self.ny, self.nz
+        S = nz * (nz + 1) // 2
+        A = nz * nz
+        out = {}
+        for c in GREEN_COMPONENTS:
+            blk = A if c in ("xz", "yz") else S
+            out[c] = np.empty((2 * nx, 2 * ny, blk), np.complex128)
+        ptrs = (C.c_void_p * 6)(*[out[c].ctypes.data for c in GREEN_COMPONENTS])
+        self.ctx._check(self.ctx.lib.egx_green_download(self.ctx.h, self.h, ptrs))
+        return out
+
+    def free(self):
+        if self.h is not None and self.ctx.h is not None:
+            self.ctx.lib.egx_green_free(self.ctx.h, self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class _ModelStruct:
+    pass
+
+
+def model_struct(model):
+    """egx_model view of a :class:`extreme_gb300.model.CartesianModel`
+    (keeps the arrays alive)."""
+    ms = _ModelStruct()
+    ms.depth = np.ascontiguousarray(model.layer_depth, np.float64)
+    ms.thick = np.ascontiguousarray(model.layer_thickness, np.float64)
+    ms.bg_t = np.ascontiguousarray(model.section.thickness, np.float64)
+    ms.bg_s = np.ascontiguousarray(model.section.sigma, np.float64)
+    dp = C.POINTER(C.c_double)
+    ms.s = Model(model.nx, model.ny, model.nz, float(model.dx), float(model.dy),
+                 ms.depth.ctypes.data_as(dp), ms.thick.ctypes.data_as(dp), len(ms.bg_t),
+                 float(model.section.zero_air_level), ms.bg_t.ctypes.data_as(dp), ms.bg_s.ctypes.data_as(dp))
+    return ms

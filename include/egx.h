@@ -1,0 +1,161 @@
+/*
+ * egx.h -- C ABI of the GB300-native integral-equation (IE) forward solve.
+ *
+ * This library replaces, behind plain C entry points, the four C# surfaces of
+ * the reference's IE hot path (prisae/extreme):
+ *
+ *   Green tensor  Extreme.Cartesian/Green/Tensor/GreenTensor.cs:14-209 and
+ *                 Extreme.Cartesian/Forward/AtoA/AtoAGreenTensorCalculatorComponent.cs:69-279
+ *   operator      Extreme.Cartesian/Forward/AtoA/ConvolutionOperator.cs:45-143
+ *                 (PrepareOperator / Apply, the mat-vec callback of FlexibleGmresSolver)
+ *   2-D FFT       Extreme.Cartesian/Fft/FftW/FftWTransform.cs:218-225 (FftWrap plan_many_dft)
+ *   solver        Extreme.Cartesian/Forward/AnomalyCurrentFgmresSolver.cs:59-85 and
+ *                 Extreme.Fgmres/FlexibleGmresWithGmresPreconditioner.cs:105-139
+ *
+ * Conventions
+ *   - complex numbers are interleaved (re, im) doubles, as System.Numerics.Complex
+ *     and the reference's complex16;
+ *   - anomaly vectors use the reference's AnomalyCurrent layout, index
+ *     ((i*ny + j)*3 + c)*nz + k (Extreme.Cartesian/Core/LayerAccessor.cs:45-47);
+ *     nrhs vectors are stored one after the other;
+ *   - every entry point returns an egx_status; errors never cross the ABI as
+ *     exceptions; egx_last_error() gives the message of the last failure;
+ *   - host buffers are owned by the caller and copied on the context stream;
+ *     calls complete synchronously. A context is not thread-safe.
+ */
+#ifndef EGX_H
+#define EGX_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    EGX_OK = 0,
+    EGX_ERR_INVALID = 1,       /* bad argument (ArgumentNullException / ArgumentOutOfRange) */
+    EGX_ERR_OOM = 2,           /* device allocation failed */
+    EGX_ERR_CUDA = 3,          /* CUDA runtime error */
+    EGX_ERR_NOT_CONVERGED = 4, /* FGMRES ran out of restarts (ResultInfo.NonConverged) */
+    EGX_ERR_TIMEOUT = 5,       /* a bounded device wait gave up */
+    EGX_ERR_STATE = 6,         /* call order (e.g. apply before prepare, InvalidOperationException) */
+    EGX_ERR_MODEL = 7          /* anomaly layer not inside one background layer (ModelUtils.cs:160-185) */
+} egx_status;
+
+enum { EGX_OP_A = 0, EGX_OP_CHI0 = 1 };             /* OperatorType.cs */
+enum { EGX_HOST = 0, EGX_DEVICE = 1 };              /* where the vectors live */
+enum { EGX_PREC_FP64 = 0, EGX_PREC_MIXED = 1 };     /* storage/arithmetic of the operator */
+enum { EGX_PRECOND_GMRES = 0, EGX_PRECOND_CALLBACK = 1, EGX_PRECOND_NONE = 2 };
+enum { EGX_FFT_FORWARD = -1, EGX_FFT_BACKWARD = 1 }; /* FFTW sign convention */
+
+typedef struct egx_ctx egx_ctx;
+typedef struct egx_green egx_green;
+
+/* Cartesian model at one frequency's geometry (CartesianModel, Section1D). */
+typedef struct {
+    int nx, ny, nz;
+    double dx, dy;                  /* lateral cell sizes, m */
+    const double *layer_depth;      /* [nz] top of each anomaly layer, m */
+    const double *layer_thickness;  /* [nz] */
+    int n_bg;                       /* background layers incl. both half-spaces */
+    double zero_air_level;          /* depth of the top of layer 0 */
+    const double *bg_thickness;     /* [n_bg]; first and last are 0 */
+    const double *bg_sigma;         /* [n_bg] conductivity, S/m */
+} egx_model;
+
+/* GmresParams + ForwardSettings (Extreme.Fgmres/GmresParams.cs:151-170,
+ * Extreme.Cartesian/Forward/Project/ForwardSettings.cs:8-12). */
+typedef struct {
+    int m_out;            /* OuterBufferLength */
+    int m_in;             /* InnerBufferLength */
+    double tol;           /* Residual */
+    int max_restarts;     /* MaxRepeatsNumber */
+    int precond;          /* EGX_PRECOND_* */
+    int check_true;       /* 1: final true-residual check (CheckWithWarning), 0: Arnoldi only */
+} egx_gmres_params;
+
+/* Mixed-precision solve: inner FGMRES in complex64 inside an FP64
+ * iterative-refinement loop (no reference counterpart; it wraps the same
+ * operator and returns the same result record). */
+typedef struct {
+    double tol;           /* target relative true residual of the outer loop */
+    int max_outer;        /* refinement steps */
+    int m_out, m_in;      /* inner FGMRES buffers */
+    double inner_tol;     /* relative tolerance of each inner solve */
+    int inner_restarts;
+} egx_mixed_params;
+
+/* ResultInfo (Extreme.Fgmres/ResultInfo.cs) plus counters. */
+typedef struct {
+    int converged;
+    int iterations;       /* outer Arnoldi steps */
+    double arnoldi_be;    /* |g_{j+1}| / ||b|| */
+    double true_be;       /* ||b - A x|| / ||b|| (-1 if not computed) */
+    int n_applies;        /* operator applications */
+    int n_refinements;    /* mixed solve only */
+} egx_result;
+
+/* Right-preconditioner callback (RightPreconditionerRequest,
+ * Extreme.Fgmres/FlexibleGmresSolver.cs:19-29): dst = M(src); device pointers
+ * of n complex values in the operator's precision. Return 0 on success. */
+typedef int (*egx_precond_fn)(void *user, const void *src, void *dst, long n, int precision);
+
+/* ---- context ----------------------------------------------------------- */
+int egx_create(int device, egx_ctx **out);
+int egx_destroy(egx_ctx *ctx);
+int egx_last_error(egx_ctx *ctx, char *buf, size_t len);
+int egx_version(void);
+/* Use an external CUDA stream (cudaStream_t) for all work of this context. */
+int egx_set_stream(egx_ctx *ctx, void *stream);
+/* Count of this library's kernel launches since the context was created. */
+long egx_launch_count(egx_ctx *ctx);
+
+/* ---- Green tensor (GreenTensor, AtoAGreenTensorCalculatorComponent) ----- */
+/* Build the anomaly-to-anomaly tensor on the device in FP64
+ * (AtoAGreenTensorCalculatorComponent.CalculateGreenTensor,
+ * AtoAGreenTensorCalculatorComponent.cs:69-89). precision: EGX_PREC_FP64
+ * keeps complex128, EGX_PREC_MIXED also keeps a complex64 copy. */
+int egx_green_build(egx_ctx *ctx, const egx_model *model, double omega, int n_hankels,
+                    int precision, egx_green **out);
+/* Upload a spectral tensor given in the reference layout: comps[6] =
+ * xx, xy, yy, zz (packed rc + tr*(tr+1)/2, Nz(Nz+1)/2 entries per point) and
+ * xz, yz (rc*Nz + tr, Nz*Nz entries), each [2nx][2ny][block] complex. */
+int egx_green_upload(egx_ctx *ctx, int nx, int ny, int nz, const double *const comps[6],
+                     int precision, egx_green **out);
+/* Download the complex128 spectral tensor in the reference layout. */
+int egx_green_download(egx_ctx *ctx, const egx_green *g, double *const comps[6]);
+int egx_green_free(egx_ctx *ctx, egx_green *g);
+
+/* ---- operator (ConvolutionOperator) ------------------------------------ */
+/* PrepareOperator (ConvolutionOperator.cs:64-143). zeta: [nx][ny][nz]
+ * complex anomaly conductivities, zeta0: [nz] complex background of each
+ * anomaly layer, dz: [nz] layer thicknesses. type: EGX_OP_A or EGX_OP_CHI0. */
+int egx_op_prepare(egx_ctx *ctx, egx_green *g, const double *zeta, const double *zeta0,
+                   const double *dz, int type);
+/* Apply (ConvolutionOperator.cs:45-62,162-327): y = K x for nrhs vectors. */
+int egx_op_apply(egx_ctx *ctx, const double *x, double *y, int nrhs, int where);
+/* Same in complex64 (interleaved floats) with the complex64 tensor. */
+int egx_op_apply_c64(egx_ctx *ctx, const float *x, float *y, int nrhs, int where);
+
+/* ---- FFT (FftWrap plan_many_dft rank 2) -------------------------------- */
+/* In-place unnormalised 2-D DFT over (n0, n1) of `howmany` interleaved
+ * sequences: element (i, j, b) at (i*n1 + j)*howmany + b. sign -1 forward. */
+int egx_fft2d(egx_ctx *ctx, double *buf, int n0, int n1, int howmany, int sign, int where);
+
+/* ---- solver (AnomalyCurrentFgmresSolver / FGMRES with GMRES precond) ---- */
+/* Solve A x = b with x holding the initial guess on entry
+ * (AnomalyCurrentFgmresSolver.Solve, FlexibleGmresWithGmresPreconditioner). */
+int egx_fgmres_solve(egx_ctx *ctx, const double *b, double *x, const egx_gmres_params *p,
+                     egx_result *res, int where);
+/* Mixed-precision form of the same solve. */
+int egx_mixed_solve(egx_ctx *ctx, const double *b, double *x, const egx_mixed_params *p,
+                    egx_result *res, int where);
+/* RightPreconditionerRequest plug point: kind EGX_PRECOND_CALLBACK routes
+ * z_j = M(v_j) of the outer FGMRES to fn(user, ...). */
+int egx_set_precond(egx_ctx *ctx, int kind, egx_precond_fn fn, void *user);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EGX_H */

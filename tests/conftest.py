@@ -1,0 +1,20 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and the built libegx.so")
+
+
+@pytest.fixture(scope="session")
+def egx_ctx():
+    from extreme_gb300 import egx
+    ctx = egx.Context(0)
+    yield ctx
+    ctx.close()
