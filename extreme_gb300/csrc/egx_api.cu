@@ -51,6 +51,7 @@ struct egx_ctx {
     // mixed-solve workspace
     DevBuf nrm_part, nrm_out, mix_r, mix_t, mix_r32, mix_d32;
     std::map<int, std::pair<std::shared_ptr<DevBuf>, FftPlan>> tw_cache;
+    GreenBuildStats last_build;
 };
 
 namespace {
@@ -214,6 +215,47 @@ long egx_launch_count(egx_ctx *ctx) {
     if (ctx->outer32) n += ctx->outer32->kernel_launches;
     if (ctx->inner32) n += ctx->inner32->kernel_launches;
     return n;
+}
+
+int egx_green_build(egx_ctx *ctx, const egx_model *model, double omega, int n_hankels, int precision,
+                    egx_green **out) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(model && out, EGX_ERR_INVALID, "null model or output");
+        EGX_CHECK(model->layer_depth && model->layer_thickness && model->bg_thickness && model->bg_sigma,
+                  EGX_ERR_INVALID, "null model arrays");
+        EGX_CHECK(omega > 0, EGX_ERR_INVALID, "omega must be positive");
+        set_device(ctx);
+        GreenModel gm;
+        gm.nx = model->nx;
+        gm.ny = model->ny;
+        gm.nz = model->nz;
+        gm.dx = model->dx;
+        gm.dy = model->dy;
+        gm.depth.assign(model->layer_depth, model->layer_depth + model->nz);
+        gm.thick.assign(model->layer_thickness, model->layer_thickness + model->nz);
+        gm.bg_thick.assign(model->bg_thickness, model->bg_thickness + model->n_bg);
+        gm.bg_sigma.assign(model->bg_sigma, model->bg_sigma + model->n_bg);
+        gm.zero_air_level = model->zero_air_level;
+        gm.omega = omega;
+        auto g = std::unique_ptr<egx_green>(new egx_green());
+        g->nx = gm.nx;
+        g->ny = gm.ny;
+        g->nz = gm.nz;
+        GreenBuildStats st;
+        build_green(gm, n_hankels, ctx->stream, g->g64, &st, &ctx->launches);
+        if (precision == EGX_PREC_MIXED) {
+            GreenDims gd{gm.nx, gm.ny, gm.nz};
+            long n = gd.Q() * gd.Bs();
+            g->g32.ensure(n * sizeof(float2));
+            convert_d2f(g->g64.as<double2>(), g->g32.as<float2>(), n, 1.0, ctx->stream);
+            ctx->launches++;
+            g->has32 = true;
+        }
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->last_build = st;
+        *out = g.release();
+    });
 }
 
 int egx_green_upload(egx_ctx *ctx, int nx, int ny, int nz, const double *const comps[6], int precision,

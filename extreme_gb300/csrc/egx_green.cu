@@ -1,9 +1,845 @@
-// Anomaly-to-anomaly Green tensor build on the device.
-#include "egx_green.cuh"
+// Anomaly-to-anomaly Green tensor, FP64, on the device.
+//
+// Host: radius plan and lambdas (ScalarPlansCreater.cs:102-176, ScalarPlan.cs:460-481),
+// merge of the plan items (InnerResultsCombiner.cs:19-61), transceiver lists
+// (TranceiverUtils.cs:55-74), knots and face integral factors
+// (GreenTensorCalculator.cs:166-437, IntegralFactors.cs:17-30), gathered per
+// cell into sparse weight lists.
+// Device, per tensor half (asym: xz, yz; symm: xx, xy, yy, zz):
+//   k_layers   per lambda: eta, exp, P/Q reflection recursions of both modes
+//              (PlanCalculatorFast.cs:203-318, green_scalar.c:30-41);
+//   k_kernels  per (transceiver, lambda): exponential sums, propagators and
+//              the kernels U1..U5 with their pre-Hankel normalisation
+//              (VolumeToVolumeCalculatorUFast.cs:34-337, green_scalar.c:86-386,
+//              ScalarMathUtils.cs:243-263);
+//   k_hankel   the 431-tap digital filter and the post normalisation
+//              (HankelCoefficients.cs:103-118, ScalarMathUtils.cs:189-207);
+//   k_segments linear pieces per radius interval (ScalarSegments.cs:86-128);
+//   k_cells    per (cell, block entry): signed sum of face integrals, written
+//              with the parity mirroring into the 2Nx x 2Ny grid
+//              (GreenTensorCalculator.cs:460-552, GreenTensorFftPopulator.cs:221-273);
+//   FFT        y then x (only the ky <= Ny columns, kx <= Nx rows kept);
+//   k_extract  the (Nx+1)(Ny+1) quadrant into the operator's block layout.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
 
-extern "C" int egx_green_build(egx_ctx *ctx, const egx_model *model, double omega, int n_hankels, int precision,
-                               egx_green **out) {
-    (void)ctx; (void)model; (void)omega; (void)n_hankels; (void)precision;
-    if (out) *out = nullptr;
-    return EGX_ERR_STATE;
+#include "egx_green.cuh"
+#include "egx_operator.cuh"
+#include "hankel_ndec40.inc"
+
+namespace egx {
+
+namespace {
+
+constexpr double kMu0 = 4.0 * M_PI * 1.0e-7;
+constexpr double kEps0 = 1.0 / (kMu0 * 299792458.0 * 299792458.0);
+constexpr int kTaps = 431;
+constexpr int kL2 = 130;
+constexpr int kMaxLayers = 32;
+
+__constant__ double c_h0[kTaps];
+__constant__ double c_h1[kTaps];
+
+typedef std::complex<double> cd;
+
+// ---------------------------------------------------------------- device math
+__device__ __forceinline__ double2 dmk(double a, double b) { return make_double2(a, b); }
+__device__ __forceinline__ double2 dadd(double2 a, double2 b) { return dmk(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 dsub(double2 a, double2 b) { return dmk(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 dmul(double2 a, double2 b) { return dmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ double2 dscal(double s, double2 a) { return dmk(s * a.x, s * a.y); }
+__device__ __forceinline__ double2 dneg(double2 a) { return dmk(-a.x, -a.y); }
+__device__ __forceinline__ double2 ddiv(double2 a, double2 b) { return cdiv<double>(a, b); }
+__device__ __forceinline__ double2 drecip(double2 b) { return cdiv<double>(dmk(1.0, 0.0), b); }
+__device__ __forceinline__ double2 dexp(double2 z) {
+    double s, c;
+    sincos(z.y, &s, &c);
+    double e = exp(z.x);
+    return dmk(e * c, e * s);
 }
+// Principal square root; the sign of a zero imaginary part selects the
+// branch on the negative real axis (C99 csqrt).
+__device__ __forceinline__ double2 dsqrt(double2 z) {
+    double x = z.x, y = z.y;
+    if (x == 0.0 && y == 0.0) return dmk(0.0, y);
+    double t = sqrt((fabs(x) + hypot(x, y)) * 0.5);
+    if (x >= 0.0) return dmk(t, y / (2.0 * t));
+    return dmk(fabs(y) / (2.0 * t), copysign(t, y));
+}
+
+struct LayerArgs {
+    int L;
+    double omega;
+    double2 zeta[kMaxLayers];
+    double2 alpha_s[kMaxLayers];
+    double2 beta_s[kMaxLayers];
+    double thick[kMaxLayers];
+    double tops[kMaxLayers + 1];
+};
+
+// Per lambda: eta, exp, P1, Q1, Ps, Qs over all layers. Arrays [6][L][nl].
+__global__ void k_layers(const double *__restrict__ lam, int nl, const LayerArgs a, double2 *__restrict__ out) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nl) return;
+    const int L = a.L;
+    double2 eta[kMaxLayers], ex[kMaxLayers];
+    const double l = lam[m];
+    for (int k = 0; k < L; k++) {
+        // value = (i*omega) * zeta * mu0, then lambda^2 - value with -Im(value)
+        double2 io = dmk(0.0, a.omega);
+        double2 v = dmul(io, a.zeta[k]);
+        v = dmk(v.x * kMu0, v.y * kMu0);
+        eta[k] = dsqrt(dmk(l * l - v.x, -v.y));
+        ex[k] = dexp(dscal(-2.0 * a.thick[k], eta[k]));
+    }
+    double2 *Eta = out, *Ex = out + (long)L * nl, *P1 = out + 2L * L * nl, *Q1 = out + 3L * L * nl;
+    double2 *Ps = out + 4L * L * nl, *Qs = out + 5L * L * nl;
+    for (int k = 0; k < L; k++) {
+        Eta[(long)k * nl + m] = eta[k];
+        Ex[(long)k * nl + m] = ex[k];
+    }
+    for (int mode = 0; mode < 2; mode++) {
+        double2 p[kMaxLayers], q[kMaxLayers];
+        for (int k = 0; k < L; k++) p[k] = q[k] = dmk(0, 0);
+        if (mode == 0) p[1] = ddiv(dsub(eta[1], eta[0]), dadd(eta[1], eta[0]));
+        else {
+            double2 a0 = dmul(a.zeta[0], eta[1]), a1 = dmul(a.zeta[1], eta[0]);
+            p[1] = ddiv(dsub(a0, a1), dadd(a0, a1));
+        }
+        for (int k = 1; k < L - 1; k++) {
+            double2 pexp = dmul(p[k], ex[k]);
+            double2 ae = ddiv(eta[k], eta[k + 1]);
+            if (mode == 1) ae = dmul(a.alpha_s[k], ae);
+            double2 part = dmul(ae, ddiv(dsub(pexp, dmk(1, 0)), dadd(pexp, dmk(1, 0))));
+            p[k + 1] = ddiv(dadd(dmk(1, 0), part), dsub(dmk(1, 0), part));
+        }
+        const int n = L - 1;
+        {
+            double2 be = ddiv(eta[n], eta[n - 1]);
+            if (mode == 1) be = dmul(a.beta_s[n], be);
+            q[n - 1] = ddiv(dsub(dmk(1, 0), be), dadd(dmk(1, 0), be));
+        }
+        for (int k = n - 1; k > 1; k--) {
+            double2 qexp = dmul(q[k], ex[k]);
+            double2 be = ddiv(eta[k], eta[k - 1]);
+            if (mode == 1) be = dmul(a.beta_s[k], be);
+            double2 part = dmul(be, ddiv(dsub(qexp, dmk(1, 0)), dadd(qexp, dmk(1, 0))));
+            q[k - 1] = ddiv(dadd(dmk(1, 0), part), dsub(dmk(1, 0), part));
+        }
+        double2 *P = mode == 0 ? P1 : Ps, *Q = mode == 0 ? Q1 : Qs;
+        for (int k = 0; k < L; k++) {
+            P[(long)k * nl + m] = p[k];
+            Q[(long)k * nl + m] = q[k];
+        }
+    }
+}
+
+struct Trans {
+    double r1, r2, s1, s2;
+    int r, s;      // background layers of receiver / transmitter
+    int kase;      // 0 match, 1 receiver below, 2 receiver above
+};
+
+// which kernels: bit0 U1, bit1 U2, bit2 U3, bit3 U4, bit4 U5; outputs packed
+// in that order, each [ntrans][nl_total] at column offset `col0`.
+__global__ void k_kernels(const double *__restrict__ lam, int nl, const double2 *__restrict__ lay, const LayerArgs a,
+                          const Trans *__restrict__ trans, int ntrans, int which, double2 *__restrict__ U,
+                          long nl_total, long col0) {
+    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)ntrans * nl) return;
+    const int tr = (int)(idx / nl);
+    const int m = (int)(idx - (long)tr * nl);
+    const Trans T0 = trans[tr];
+    const int L = a.L;
+    const double2 *Eta = lay, *Ex = lay + (long)L * nl, *P1 = lay + 2L * L * nl, *Q1 = lay + 3L * L * nl;
+    const double2 *Ps = lay + 4L * L * nl, *Qs = lay + 5L * L * nl;
+#define E(k) Eta[(long)(k) * nl + m]
+#define X(k) Ex[(long)(k) * nl + m]
+    const int r = T0.r, s = T0.s, t = min(r, s), b = max(r, s);
+    const double dt = a.tops[t], db1 = a.tops[b + 1];
+    const double r1 = T0.r1, r2 = T0.r2, s1 = T0.s1, s2 = T0.s2;
+    const double2 er = E(r), es = E(s), et = E(t), eb = E(b);
+    const double l = lam[m];
+    auto lin3 = [](double c1, double2 v1, double c2, double2 v2, double c3, double2 v3) {
+        double2 acc = dscal(c1, v1);
+        acc = dadd(acc, dscal(c2, v2));
+        return dadd(acc, dscal(c3, v3));
+    };
+    auto lin2 = [](double c1, double2 v1, double c2, double2 v2) { return dadd(dscal(c1, v1), dscal(c2, v2)); };
+    // CalculateT / CalculateR
+    double2 Tt = dexp(lin3(-r1, er, -s1, es, 2 * dt, et));
+    Tt = dsub(Tt, dexp(lin3(-r1, er, -s2, es, 2 * dt, et)));
+    Tt = dsub(Tt, dexp(lin3(-r2, er, -s1, es, 2 * dt, et)));
+    Tt = dadd(Tt, dexp(lin3(-r2, er, -s2, es, 2 * dt, et)));
+    double2 Rr = dexp(lin3(-2 * db1, eb, s2, es, r2, er));
+    Rr = dsub(Rr, dexp(lin3(-2 * db1, eb, s1, es, r2, er)));
+    Rr = dsub(Rr, dexp(lin3(-2 * db1, eb, s2, es, r1, er)));
+    Rr = dadd(Rr, dexp(lin3(-2 * db1, eb, s1, es, r1, er)));
+    double2 C = dmk(0, 0), D = dmk(0, 0);
+    if (T0.kase == 2) {  // receiver above: CTop, DTop
+        C = dexp(lin2(-s1, es, r2, er));
+        C = dsub(C, dexp(lin2(-s2, es, r2, er)));
+        C = dsub(C, dexp(lin2(-s1, es, r1, er)));
+        C = dadd(C, dexp(lin2(-s2, es, r1, er)));
+        double2 F = lin2(-2 * db1, eb, 2 * dt, et);
+        D = dexp(dadd(dadd(F, dscal(s2, es)), dscal(-r1, er)));
+        D = dsub(D, dexp(dadd(dadd(F, dscal(s1, es)), dscal(-r1, er))));
+        D = dsub(D, dexp(dadd(dadd(F, dscal(s2, es)), dscal(-r2, er))));
+        D = dadd(D, dexp(dadd(dadd(F, dscal(s1, es)), dscal(-r2, er))));
+    } else if (T0.kase == 1) {  // receiver below: CBot, DBot
+        C = dexp(lin2(-r1, er, s2, es));
+        C = dsub(C, dexp(lin2(-r1, er, s1, es)));
+        C = dsub(C, dexp(lin2(-r2, er, s2, es)));
+        C = dadd(C, dexp(lin2(-r2, er, s1, es)));
+        double2 F = lin2(-2 * db1, eb, 2 * dt, et);
+        D = dexp(dadd(dadd(F, dscal(-s1, es)), dscal(r2, er)));
+        D = dsub(D, dexp(dadd(dadd(F, dscal(-s2, es)), dscal(r2, er))));
+        D = dsub(D, dexp(dadd(dadd(F, dscal(-s1, es)), dscal(r1, er))));
+        D = dadd(D, dexp(dadd(dadd(F, dscal(-s2, es)), dscal(r1, er))));
+    }
+    // propagator chain A[t, b] of a mode
+    auto chain = [&](const double2 *P, const double2 *Q) {
+        double2 A = drecip(dmul(E(b), dsub(dmk(1, 0), dmul(dmul(P[(long)b * nl + m], Q[(long)b * nl + m]), X(b)))));
+        for (int k = b - 1; k >= t; k--) {
+            double2 num = dadd(dmk(1, 0), P[(long)(k + 1) * nl + m]);
+            double2 den = dadd(dmk(1, 0), dmul(P[(long)k * nl + m], X(k)));
+            double2 f = dmul(ddiv(num, den), dexp(dscal(a.tops[k + 1], dsub(E(k + 1), E(k)))));
+            A = dmul(f, A);
+        }
+        return A;
+    };
+    auto psi1 = [&](const double2 *P, const double2 *Q) {
+        double2 pt = P[(long)t * nl + m], qb = Q[(long)b * nl + m];
+        if (T0.kase == 0) {
+            const int n = r;
+            const double tau = r2 - r1;
+            const double dn1 = a.tops[n + 1] - a.tops[n];
+            double2 en = E(n);
+            double2 part1 = dsub(dscal(tau, en), dsub(dmk(1, 0), dexp(dscal(-tau, en))));
+            double2 pq = dmul(P[(long)n * nl + m], Q[(long)n * nl + m]);
+            double2 e1 = dexp(dscal(-2 * dn1, en));
+            double2 e2 = dexp(dadd(dscal(-2 * dn1, en), dscal(tau, en)));
+            double2 part2 = dmul(pq, dsub(dmul(dadd(dscal(tau, en), dmk(1, 0)), e1), e2));
+            return dscal(2.0, dsub(part1, part2));
+        }
+        return dadd(C, dmul(dmul(pt, qb), D));
+    };
+    auto psi3 = [&](const double2 *P, const double2 *Q) {
+        if (T0.kase == 0) return dmk(0, 0);
+        double2 pqd = dmul(dmul(P[(long)t * nl + m], Q[(long)b * nl + m]), D);
+        if (T0.kase == 1) return dadd(dneg(C), pqd);
+        return dsub(C, pqd);
+    };
+    auto special = [&](const double2 *P, const double2 *Q, double psign, double psisign, double2 psi) {
+        double2 v = dmul(dscal(psign, P[(long)t * nl + m]), Tt);
+        v = dadd(v, dmul(Q[(long)b * nl + m], Rr));
+        return dadd(v, dscal(psisign, psi));
+    };
+    const double2 annf = drecip(dmul(er, es));
+    const double2 zr2 = dscal(2.0, a.zeta[r]);
+    long out = 0;
+    double2 *Ub = U + (long)tr * nl_total + col0 + m;
+    const long ustride = (long)ntrans * nl_total;
+    if (which & 1) {
+        double2 ann = chain(P1, Q1);
+        double2 u = dmul(dmul(ann, annf), special(P1, Q1, 1, 1, psi1(P1, Q1)));
+        u = dmul(u, dmk(0.0, a.omega * kMu0 * 0.5));
+        Ub[ustride * out++] = u;
+    }
+    double2 anns = chain(Ps, Qs);
+    if (r > s) anns = dmul(ddiv(a.zeta[r], a.zeta[s]), anns);
+    if (which & 2) {
+        double2 u = dmul(anns, special(Ps, Qs, 1, -1, psi1(Ps, Qs)));
+        Ub[ustride * out++] = ddiv(u, zr2);
+    }
+    if (which & 4) {
+        double2 u = dmul(dmul(anns, drecip(es)), special(Ps, Qs, -1, 1, psi3(Ps, Qs)));
+        Ub[ustride * out++] = dmul(u, ddiv(dmk(l, 0), zr2));
+    }
+    if (which & 8) {
+        double2 u = dmul(dmul(anns, drecip(er)), special(Ps, Qs, -1, -1, psi3(Ps, Qs)));
+        Ub[ustride * out++] = dmul(u, ddiv(dmk(-l, 0), zr2));
+    }
+    if (which & 16) {
+        double2 u;
+        if (T0.kase == 0) {
+            const int n = r;
+            const double tau = r2 - r1;
+            const double ln = a.thick[n];
+            double2 en = E(n);
+            double2 kk = dmk(-a.omega * kMu0 * a.zeta[n].y, a.omega * kMu0 * a.zeta[n].x);
+            double2 pq = dmul(Ps[(long)n * nl + m], Qs[(long)n * nl + m]);
+            double2 part1 = dneg(dsub(dmk(1, 0), dexp(dscal(-tau, en))));
+            double2 part2 = dmul(pq, dsub(dexp(dscal(-(2 * ln - tau), en)), dexp(dscal(-2 * ln, en))));
+            double2 part3 = dmul(dmul(dscal(1.0 / (l * l), kk), dsub(dmk(1, 0), dmul(pq, dexp(dscal(-2 * ln, en))))),
+                                 dscal(tau, en));
+            double2 psi5 = dscal(2.0, dadd(dadd(part1, part2), part3));
+            double2 sp = dadd(dadd(dmul(Ps[(long)t * nl + m], Tt), dmul(Qs[(long)b * nl + m], Rr)), psi5);
+            u = dmul(dmul(anns, annf), sp);
+        } else {
+            u = dmul(dmul(anns, annf), special(Ps, Qs, 1, 1, psi1(Ps, Qs)));
+        }
+        Ub[ustride * out++] = dmul(u, ddiv(dmk(l * l, 0), zr2));
+    }
+#undef E
+#undef X
+}
+
+// I[u][trans][g] = norm * sum_j h[430 - j] * U[u][trans][col0 + i + j]
+__global__ void k_hankel(const double2 *__restrict__ U, int nu, int ntrans, long nl_total, long col0, int nrho,
+                         const double *__restrict__ rho, const int *__restrict__ gidx, const int *__restrict__ use_h0,
+                         const int *__restrict__ negate, double2 *__restrict__ I, int nrad) {
+    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)nu * ntrans * nrho) return;
+    int i = (int)(idx % nrho);
+    long rest = idx / nrho;
+    int tr = (int)(rest % ntrans);
+    int u = (int)(rest / ntrans);
+    const double2 *f = U + ((long)u * ntrans + tr) * nl_total + col0 + i;
+    const double *h = use_h0[u] ? c_h0 : c_h1;
+    double sx = 0, sy = 0;
+    for (int j = 0; j < kTaps; j++) {
+        double hj = h[kTaps - 1 - j];
+        double2 v = f[j];
+        sx += v.x * hj;
+        sy += v.y * hj;
+    }
+    double den = 2.0 * M_PI * rho[i];
+    if (negate[u]) {
+        sx = -sx;
+        sy = -sy;
+    }
+    I[((long)u * ntrans + tr) * nrad + gidx[i]] = dmk(sx / den, sy / den);
+}
+
+// IA/IB[u][seg][trans]
+__global__ void k_segments(const double2 *__restrict__ I, int nu, int ntrans, int nrad, const double *__restrict__ radii,
+                           double2 *__restrict__ IA, double2 *__restrict__ IB) {
+    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nseg = nrad - 1;
+    if (idx >= (long)nu * nseg * ntrans) return;
+    int tr = (int)(idx % ntrans);
+    long rest = idx / ntrans;
+    int sg = (int)(rest % nseg);
+    int u = (int)(rest / nseg);
+    const double2 *v = I + ((long)u * ntrans + tr) * nrad;
+    double sr = radii[sg], ur = radii[sg + 1];
+    double div = ur - sr;
+    double2 a = dmk((v[sg + 1].x - v[sg].x) / div, (v[sg + 1].y - v[sg].y) / div);
+    double2 bb = dsub(v[sg], dmul(a, dmk(sr, 0)));
+    long o = ((long)u * nseg + sg) * ntrans + tr;
+    IA[o] = a;
+    IB[o] = bb;
+}
+
+struct Term {
+    int seg;
+    int src;
+    double wa, wb;
+};
+
+// Real-space value of each quadrant cell for block entries [t0, t0+tc),
+// written with the parity mirroring into buf[2nx][2ny][tc].
+__global__ void k_cells(const int *__restrict__ rowptr, const Term *__restrict__ terms, const double2 *__restrict__ IA,
+                        const double2 *__restrict__ IB, int ntrans, int nseg, int nx, int ny, int t0, int tc, int xs,
+                        int ys, double2 *__restrict__ buf) {
+    const int cell = blockIdx.x;
+    const int i = cell / ny, j = cell - (cell / ny) * ny;
+    const int t = blockIdx.y * blockDim.x + threadIdx.x;
+    if (t >= tc) return;
+    double2 acc = dmk(0, 0);
+    for (int e = rowptr[cell]; e < rowptr[cell + 1]; e++) {
+        const Term tm = terms[e];
+        long o = ((long)tm.src * nseg + tm.seg) * ntrans + t0 + t;
+        double2 a = IA[o], b = IB[o];
+        acc.x = fma(tm.wa, a.x, acc.x);
+        acc.y = fma(tm.wa, a.y, acc.y);
+        acc.x = fma(tm.wb, b.x, acc.x);
+        acc.y = fma(tm.wb, b.y, acc.y);
+    }
+    const int n0 = 2 * nx, n1 = 2 * ny;
+    buf[((long)i * n1 + j) * tc + t] = acc;
+    if (i >= 1 && j >= 1) {
+        buf[((long)(n0 - i) * n1 + j) * tc + t] = dscal((double)xs, acc);
+        buf[((long)i * n1 + (n1 - j)) * tc + t] = dscal((double)ys, acc);
+        buf[((long)(n0 - i) * n1 + (n1 - j)) * tc + t] = dscal((double)(xs * ys), acc);
+    } else if (i >= 1) {
+        buf[((long)(n0 - i) * n1) * tc + t] = dscal((double)xs, acc);
+    } else if (j >= 1) {
+        buf[((long)(n1 - j)) * tc + t] = dscal((double)ys, acc);
+    }
+}
+
+__global__ void k_extract(const double2 *__restrict__ buf, int nx, int ny, int tc, int Bs, int off,
+                          double2 *__restrict__ quad) {
+    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    long total = (long)(nx + 1) * (ny + 1) * tc;
+    if (idx >= total) return;
+    int t = (int)(idx % tc);
+    long q = idx / tc;
+    int a = (int)(q / (ny + 1)), b = (int)(q - (long)a * (ny + 1));
+    quad[q * Bs + off + t] = buf[((long)a * 2 * ny + b) * tc + t];
+}
+
+// ---------------------------------------------------------------- host plan
+double rho_step() {
+    float e = 1.0f / 40.0f;
+    return (double)(float)std::pow(10.0, (double)e);
+}
+
+std::vector<double> rho_from_min(double mn, double mx, double step) {
+    std::vector<double> out;
+    double r = mn;
+    while (r <= mx) {
+        out.push_back(r);
+        r *= step;
+    }
+    out.push_back(r);
+    return out;
+}
+
+std::vector<double> rho_from_max(double mn, double mx, double step) {
+    std::vector<double> out;
+    double r = mx;
+    while (r >= mn) {
+        out.push_back(r);
+        r /= step;
+    }
+    out.push_back(r);
+    std::reverse(out.begin(), out.end());
+    return out;
+}
+
+std::vector<double> lambdas_for(const std::vector<double> &rho, double step) {
+    int n = kTaps + (int)rho.size();
+    std::vector<double> k(n);
+    k[kL2] = 1.0 / rho[0];
+    for (int i = kL2 + 1; i < n; i++) k[i] = k[i - 1] / step;
+    for (int i = kL2 - 1; i >= 0; i--) k[i] = k[i + 1] * step;
+    return k;
+}
+
+struct Knot {
+    int idx;
+    double r;
+};
+
+Knot make_knot(const std::vector<double> &radii, double x, double y) {
+    double r = std::sqrt(x * x + y * y);
+    int idx = (int)(std::upper_bound(radii.begin(), radii.end(), r) - radii.begin()) - 1;
+    if (idx == (int)radii.size() - 1) idx--;
+    if (idx < 0) idx = 0;
+    return Knot{idx, r};
+}
+
+struct Factors {
+    double d1a, d1b, d2a, d2b, d3a, d3b;
+};
+
+Factors integral_factors(double s, double u, double rs, double ru, double v) {
+    Factors f;
+    if (v == 0) {
+        f.d1a = (u * ru - s * rs) / 2;
+        f.d2a = 0;
+        f.d2b = 0;
+    } else {
+        double lg = std::log((u + ru) / (s + rs));
+        f.d1a = (u * ru - s * rs + v * v * lg) / 2;
+        f.d2a = -(u - s) * v;
+        f.d2b = -(v * lg);
+    }
+    f.d1b = u - s;
+    f.d3a = -(u * u - s * s) / 2;
+    f.d3b = -(ru - rs);
+    return f;
+}
+
+struct SegF {
+    int seg;
+    Factors f;
+};
+
+void integrate(const std::vector<double> &radii, Knot left, Knot right, double s, double u, double v,
+               std::vector<SegF> &out) {
+    out.clear();
+    if (left.idx == right.idx) {
+        out.push_back({left.idx, integral_factors(s, u, left.r, right.r, v)});
+        return;
+    }
+    double r1 = left.r, r2 = radii[left.idx + 1];
+    double sj = s, uj = std::sqrt(r2 * r2 - v * v);
+    out.push_back({left.idx, integral_factors(sj, uj, r1, r2, v)});
+    for (int i = left.idx + 1; i < right.idx; i++) {
+        r1 = r2;
+        r2 = radii[i + 1];
+        sj = uj;
+        uj = std::sqrt(r2 * r2 - v * v);
+        out.push_back({i, integral_factors(sj, uj, r1, r2, v)});
+    }
+    sj = uj;
+    uj = u;
+    r1 = r2;
+    r2 = right.r;
+    out.push_back({right.idx, integral_factors(sj, uj, r1, r2, v)});
+}
+
+// component index: 0 xx, 1 xy, 2 yy, 3 zz, 4 xz, 5 yz
+// QSigns (QSign.cs:254-257) in that order
+const int kQX[6] = {1, -1, -1, -1, 1, 1};
+const int kQY[6] = {-1, -1, 1, -1, 1, 1};
+const int kQXS[6] = {1, 1, -1, -1, -1, 1};
+const int kQYS[6] = {-1, 1, 1, -1, 1, -1};
+// (factor 1/2/3, source scalar) per direction (AddToQBuffAlong{X,Y}Electric);
+// source: 1 I1, 2 I2, 3 I3, 5 I5; 0 = component not filled in that direction
+const int kFacX[6] = {2, 3, 2, 2, 0, 1}, kSrcX[6] = {1, 2, 2, 5, 0, 3};
+const int kFacY[6] = {2, 3, 2, 2, 1, 0}, kSrcY[6] = {2, 1, 1, 5, 3, 0};
+
+double fac_a(const Factors &f, int k) { return k == 1 ? f.d1a : (k == 2 ? f.d2a : f.d3a); }
+double fac_b(const Factors &f, int k) { return k == 1 ? f.d1b : (k == 2 ? f.d2b : f.d3b); }
+
+// Per-cell term lists of one component.
+void cell_terms(const GreenModel &m, const std::vector<double> &radii, int comp, const int *src_slot,
+                std::vector<int> &rowptr, std::vector<Term> &terms) {
+    const int nx = m.nx, ny = m.ny;
+    const double dx = m.dx, dy = m.dy;
+    std::vector<Knot> kn((size_t)(nx + 1) * (ny + 1));
+    for (int i = 0; i <= nx; i++)
+        for (int j = 0; j <= ny; j++) kn[(size_t)i * (ny + 1) + j] = make_knot(radii, dx * (i - 0.5), dy * (j - 0.5));
+    std::vector<Knot> zx(ny + 1), zy(nx + 1);
+    for (int j = 0; j <= ny; j++) zx[j] = make_knot(radii, 0.0, dy * (j - 0.5));
+    for (int i = 0; i <= nx; i++) zy[i] = make_knot(radii, dx * (i - 0.5), 0.0);
+    auto K = [&](int i, int j) { return kn[(size_t)i * (ny + 1) + j]; };
+    std::vector<std::vector<Term>> per((size_t)nx * ny);
+    std::vector<SegF> parts;
+    auto add = [&](int dir, bool symm, int i, int j, int sign) {
+        const int fac = dir == 0 ? kFacX[comp] : kFacY[comp];
+        const int src = dir == 0 ? kSrcX[comp] : kSrcY[comp];
+        const int q = dir == 0 ? (symm ? kQXS[comp] : kQX[comp]) : (symm ? kQYS[comp] : kQY[comp]);
+        const double w = (double)(sign * q);
+        auto &lst = per[(size_t)i * ny + j];
+        for (const SegF &p : parts) lst.push_back(Term{p.seg, src_slot[src], w * fac_a(p.f, fac), w * fac_b(p.f, fac)});
+    };
+    auto fill_x = [&](bool symm, int i, int j) {
+        if (j == 0) add(0, symm, i, 0, -1);
+        else if (j == ny) add(0, symm, i, ny - 1, 1);
+        else {
+            add(0, symm, i, j - 1, 1);
+            add(0, symm, i, j, -1);
+        }
+    };
+    auto fill_y = [&](bool symm, int i, int j) {
+        if (i == 0) add(1, symm, 0, j, -1);
+        else if (i == nx) add(1, symm, nx - 1, j, 1);
+        else {
+            add(1, symm, i - 1, j, 1);
+            add(1, symm, i, j, -1);
+        }
+    };
+    if (kFacX[comp]) {
+        for (int j = 0; j <= ny; j++) {
+            double y = dy * (j - 0.5);
+            for (int i = 0; i < nx; i++) {
+                double x1 = dx * (i - 0.5), x2 = dx * (i + 0.5);
+                if (x1 > 0 && x2 > 0) {
+                    integrate(radii, K(i, j), K(i + 1, j), x1, x2, y, parts);
+                    fill_x(false, i, j);
+                } else if (x1 < 0 && x2 < 0) {
+                    integrate(radii, K(i + 1, j), K(i, j), -x2, -x1, y, parts);
+                    fill_x(true, i, j);
+                } else {
+                    integrate(radii, zx[j], K(i, j), 0.0, -x1, y, parts);
+                    fill_x(true, i, j);
+                    integrate(radii, zx[j], K(i + 1, j), 0.0, x2, y, parts);
+                    fill_x(false, i, j);
+                }
+            }
+        }
+    }
+    if (kFacY[comp]) {
+        for (int i = 0; i <= nx; i++) {
+            double x = dx * (i - 0.5);
+            for (int j = 0; j < ny; j++) {
+                double y1 = dy * (j - 0.5), y2 = dy * (j + 0.5);
+                if (y1 > 0 && y2 > 0) {
+                    integrate(radii, K(i, j), K(i, j + 1), y1, y2, x, parts);
+                    fill_y(false, i, j);
+                } else if (y1 < 0 && y2 < 0) {
+                    integrate(radii, K(i, j + 1), K(i, j), -y2, -y1, x, parts);
+                    fill_y(true, i, j);
+                } else {
+                    integrate(radii, zy[i], K(i, j), 0.0, -y1, x, parts);
+                    fill_y(true, i, j);
+                    integrate(radii, zy[i], K(i, j + 1), 0.0, y2, x, parts);
+                    fill_y(false, i, j);
+                }
+            }
+        }
+    }
+    rowptr.assign((size_t)nx * ny + 1, 0);
+    terms.clear();
+    for (size_t c = 0; c < per.size(); c++) {
+        rowptr[c] = (int)terms.size();
+        terms.insert(terms.end(), per[c].begin(), per[c].end());
+    }
+    rowptr[per.size()] = (int)terms.size();
+}
+
+int layer_of(const std::vector<double> &tops, const std::vector<double> &thick, double depth) {
+    double prev = tops[0];
+    for (size_t k = 0; k < thick.size(); k++) {
+        double d1 = prev, d2 = prev + thick[k];
+        if (depth >= d1 && depth < d2) return (int)k;
+        prev = d2;
+    }
+    throw Error(EGX_ERR_MODEL, "anomaly is not within the 1-D section");
+}
+
+template <typename X>
+X *dev_upload(DevBuf &b, const std::vector<X> &v, cudaStream_t s) {
+    b.ensure(std::max<size_t>(1, v.size()) * sizeof(X));
+    if (!v.empty()) EGX_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(X), cudaMemcpyHostToDevice, s));
+    return b.as<X>();
+}
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+std::vector<int> background_indices(const GreenModel &m) {
+    std::vector<int> out(m.nz);
+    for (int k = 0; k < m.nz; k++) {
+        double start = m.depth[k], end = m.depth[k] + m.thick[k];
+        double ss = m.zero_air_level;
+        int found = -1;
+        for (size_t i = 0; i < m.bg_thick.size(); i++) {
+            double es = ss + m.bg_thick[i];
+            if (start >= ss && end <= es) {
+                found = (int)i;
+                break;
+            }
+            ss = es;
+        }
+        if (found < 0)
+            throw Error(EGX_ERR_MODEL, "anomaly layer " + std::to_string(k) + " is not inside one background layer");
+        out[k] = found;
+    }
+    return out;
+}
+
+void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &quad, GreenBuildStats *stats,
+                 long *launches) {
+    auto t_start = std::chrono::steady_clock::now();
+    EGX_CHECK(m.nx > 0 && m.ny > 0 && m.nz > 0 && m.dx > 0 && m.dy > 0, EGX_ERR_INVALID, "bad model dimensions");
+    const int L = (int)m.bg_thick.size();
+    EGX_CHECK(L >= 3 && L <= kMaxLayers, EGX_ERR_INVALID, "background must have 3.." + std::to_string(kMaxLayers) +
+                                                              " layers including both half-spaces");
+    background_indices(m);
+    static bool taps_loaded = false;
+    if (!taps_loaded) {
+        EGX_CUDA(cudaMemcpyToSymbol(c_h0, kHankelJ0, sizeof(kHankelJ0)));
+        EGX_CUDA(cudaMemcpyToSymbol(c_h1, kHankelJ1, sizeof(kHankelJ1)));
+        taps_loaded = true;
+    }
+    // ---- background
+    LayerArgs la{};
+    la.L = L;
+    la.omega = m.omega;
+    std::vector<double> tops(L + 1);
+    tops[0] = m.zero_air_level;
+    for (int k = 0; k < L; k++) tops[k + 1] = tops[k] + m.bg_thick[k];
+    std::vector<cd> zb(L);
+    for (int k = 0; k < L; k++) {
+        zb[k] = cd(m.bg_sigma[k], -m.omega * kEps0);
+        la.zeta[k] = make_double2(zb[k].real(), zb[k].imag());
+        la.thick[k] = m.bg_thick[k];
+        la.tops[k] = tops[k];
+    }
+    la.tops[L] = tops[L];
+    for (int k = 0; k < L - 1; k++) {
+        cd v = zb[k + 1] / zb[k];
+        la.alpha_s[k] = make_double2(v.real(), v.imag());
+    }
+    for (int k = 1; k < L; k++) {
+        cd v = zb[k - 1] / zb[k];
+        la.beta_s[k] = make_double2(v.real(), v.imag());
+    }
+    // ---- plan
+    const double step = rho_step();
+    const double half1 = m.dx / 2.0, half2 = m.dy / 2.0;
+    const double rho_min = std::min(half1, half2);
+    const double mxx = m.nx * m.dx - half1, mxy = m.ny * m.dy - half2;
+    const double rho_max = std::sqrt(mxx * mxx + mxy * mxy);
+    const int nh = std::abs(n_hankels);
+    EGX_CHECK(nh >= 1, EGX_ERR_INVALID, "NumberOfHankels must be non-zero");
+    std::vector<std::vector<double>> items;
+    items.push_back(rho_from_min(rho_min, rho_max, step));
+    const double r2 = items[0].back(), r1 = items[0][items[0].size() - 2];
+    const double lin = (r2 - r1) / nh;
+    for (int i = 1; i < nh; i++) items.push_back(rho_from_max(rho_min, r2 - i * lin, step));
+    // merge
+    struct RI {
+        double r;
+        int item, idx;
+    };
+    std::vector<RI> all;
+    for (int it = 0; it < (int)items.size(); it++)
+        for (int j = 0; j < (int)items[it].size(); j++) all.push_back({items[it][j], it, j});
+    std::stable_sort(all.begin(), all.end(), [](const RI &a, const RI &b) { return a.r < b.r; });
+    std::vector<double> radii(all.size());
+    std::vector<std::vector<int>> gidx(items.size());
+    for (size_t it = 0; it < items.size(); it++) gidx[it].resize(items[it].size());
+    for (size_t g = 0; g < all.size(); g++) {
+        radii[g] = all[g].r;
+        gidx[all[g].item][all[g].idx] = (int)g;
+        if (g > 0) EGX_CHECK(radii[g] != radii[g - 1], EGX_ERR_INVALID, "duplicate radii across plan items");
+    }
+    const int nrad = (int)radii.size();
+    std::vector<std::vector<double>> lams;
+    std::vector<long> col0;
+    long nl_total = 0;
+    for (auto &rho : items) {
+        lams.push_back(lambdas_for(rho, step));
+        col0.push_back(nl_total);
+        nl_total += (long)lams.back().size();
+    }
+    if (stats) {
+        stats->n_items = (int)items.size();
+        stats->n_radii = nrad;
+        stats->n_lambda = nl_total;
+    }
+    // ---- transceivers
+    std::vector<double> bthick(m.bg_thick.begin(), m.bg_thick.end());
+    auto make_trans = [&](int rc, int tr) {
+        Trans t;
+        t.r1 = m.depth[rc];
+        t.r2 = m.depth[rc] + m.thick[rc];
+        t.s1 = m.depth[tr];
+        t.s2 = m.depth[tr] + m.thick[tr];
+        double zwork = t.r1 + (t.r2 - t.r1) / 2;
+        t.r = layer_of(tops, bthick, zwork);
+        t.s = layer_of(tops, bthick, t.s1 + (t.s2 - t.s1) / 2);
+        EGX_CHECK(t.r + 1 < L && t.s + 1 < L, EGX_ERR_MODEL, "anomaly layer inside the lower half-space");
+        if (zwork > t.s1 && zwork < t.s2) t.kase = 0;
+        else if (zwork >= t.s2) t.kase = 1;
+        else t.kase = 2;
+        return t;
+    };
+    std::vector<Trans> asym, symm;
+    for (int rc = 0; rc < m.nz; rc++)
+        for (int tr = 0; tr < m.nz; tr++) asym.push_back(make_trans(rc, tr));
+    for (int tr = 0; tr < m.nz; tr++)
+        for (int rc = 0; rc <= tr; rc++) symm.push_back(make_trans(rc, tr));
+
+    GreenDims gd{m.nx, m.ny, m.nz};
+    const int Bs = gd.Bs();
+    quad.ensure((size_t)gd.Q() * Bs * sizeof(double2));
+
+    DevBuf d_lam, d_lay, d_trans, d_U, d_I, d_rho, d_gidx, d_flags, d_neg, d_radii, d_IA, d_IB, d_rowptr, d_terms,
+        d_buf;
+    FftPlan p0 = make_fft_plan(2 * m.nx), p1 = make_fft_plan(2 * m.ny);
+    DevBuf tw0, tw1;
+    {
+        std::vector<double> t0 = twiddles(2 * m.nx), t1 = twiddles(2 * m.ny);
+        dev_upload(tw0, t0, s);
+        dev_upload(tw1, t1, s);
+    }
+    double *radii_dev = dev_upload(d_radii, radii, s);
+
+    // the two halves: asym (U3 -> xz, yz), symm (U1, U2, U5 -> xx, xy, yy, zz)
+    for (int half = 0; half < 2; half++) {
+        auto t_half = std::chrono::steady_clock::now();
+        const std::vector<Trans> &tl = half == 0 ? asym : symm;
+        const int ntrans = (int)tl.size();
+        const int which = half == 0 ? 4 : (1 | 2 | 16);
+        const int nu = half == 0 ? 1 : 3;
+        std::vector<int> use_h0 = half == 0 ? std::vector<int>{1} : std::vector<int>{0, 0, 0};
+        std::vector<int> negate = half == 0 ? std::vector<int>{0} : std::vector<int>{1, 0, 0};
+        Trans *dtrans = dev_upload(d_trans, tl, s);
+        d_U.ensure((size_t)nu * ntrans * nl_total * sizeof(double2));
+        d_I.ensure((size_t)nu * ntrans * nrad * sizeof(double2));
+        int *dflags = dev_upload(d_flags, use_h0, s);
+        int *dneg = dev_upload(d_neg, negate, s);
+        for (size_t it = 0; it < items.size(); it++) {
+            const int nl = (int)lams[it].size();
+            double *dl = dev_upload(d_lam, lams[it], s);
+            d_lay.ensure((size_t)6 * L * nl * sizeof(double2));
+            k_layers<<<(nl + 127) / 128, 128, 0, s>>>(dl, nl, la, d_lay.as<double2>());
+            long nthreads = (long)ntrans * nl;
+            k_kernels<<<(unsigned)((nthreads + 127) / 128), 128, 0, s>>>(dl, nl, d_lay.as<double2>(), la, dtrans,
+                                                                          ntrans, which, d_U.as<double2>(), nl_total,
+                                                                          col0[it]);
+            const int nrho = (int)items[it].size();
+            double *drho = dev_upload(d_rho, items[it], s);
+            int *dg = dev_upload(d_gidx, gidx[it], s);
+            long nh_threads = (long)nu * ntrans * nrho;
+            k_hankel<<<(unsigned)((nh_threads + 127) / 128), 128, 0, s>>>(d_U.as<double2>(), nu, ntrans, nl_total,
+                                                                           col0[it], nrho, drho, dg, dflags, dneg,
+                                                                           d_I.as<double2>(), nrad);
+            // the per-item uploads above reuse buffers: finish before the next item
+            EGX_CUDA(cudaStreamSynchronize(s));
+            if (launches) *launches += 3;
+        }
+        const int nseg = nrad - 1;
+        d_IA.ensure((size_t)nu * nseg * ntrans * sizeof(double2));
+        d_IB.ensure((size_t)nu * nseg * ntrans * sizeof(double2));
+        {
+            long n = (long)nu * nseg * ntrans;
+            k_segments<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_I.as<double2>(), nu, ntrans, nrad, radii_dev,
+                                                                   d_IA.as<double2>(), d_IB.as<double2>());
+            if (launches) *launches += 1;
+        }
+        EGX_CUDA(cudaGetLastError());
+        EGX_CUDA(cudaStreamSynchronize(s));
+        if (stats) stats->ms_scalars += ms_since(t_half);
+        // source slot of each scalar in the IA/IB arrays of this half
+        int slot[6] = {0, 0, 1, 0, 0, 2};  // I1 -> 0, I2 -> 1, I5 -> 2 (symm); I3 -> 0 (asym)
+        const int comps_asym[2] = {4, 5}, comps_symm[4] = {0, 1, 2, 3};
+        const int *comps = half == 0 ? comps_asym : comps_symm;
+        const int ncomp = half == 0 ? 2 : 4;
+        const int blk = half == 0 ? gd.A() : gd.S();
+        const int S = gd.S(), A = gd.A();
+        const int offs[6] = {0, S, 2 * S, 3 * S, 4 * S, 4 * S + A};
+        const int px[6] = {1, -1, 1, 1, -1, 1}, py[6] = {1, -1, 1, 1, 1, -1};
+        const long cells4 = 4L * m.nx * m.ny;
+        int tc = (int)std::min<long>(blk, std::max<long>(1, (long)(1.5e9 / (cells4 * sizeof(double2)))));
+        d_buf.ensure((size_t)cells4 * tc * sizeof(double2));
+        for (int ci = 0; ci < ncomp; ci++) {
+            const int c = comps[ci];
+            auto t_int = std::chrono::steady_clock::now();
+            std::vector<int> rowptr;
+            std::vector<Term> terms;
+            cell_terms(m, radii, c, slot, rowptr, terms);
+            if (stats) stats->face_terms += (long)terms.size();
+            int *drow = dev_upload(d_rowptr, rowptr, s);
+            Term *dterm = dev_upload(d_terms, terms, s);
+            for (int t0 = 0; t0 < blk; t0 += tc) {
+                const int tcc = std::min(tc, blk - t0);
+                EGX_CUDA(cudaMemsetAsync(d_buf.p, 0, (size_t)cells4 * tcc * sizeof(double2), s));
+                dim3 grid(m.nx * m.ny, (tcc + 127) / 128);
+                k_cells<<<grid, 128, 0, s>>>(drow, dterm, d_IA.as<double2>(), d_IB.as<double2>(), ntrans, nseg, m.nx,
+                                             m.ny, t0, tcc, px[c], py[c], d_buf.as<double2>());
+                EGX_CUDA(cudaGetLastError());
+                // y along all 2nx rows; x along ky <= ny, kx <= nx kept
+                const int n0 = 2 * m.nx, n1 = 2 * m.ny;
+                fft_lines<double>(d_buf.as<double2>(), n0, (long)n1 * tcc, tcc, tcc, n1, n1, p1, tw1.as<double2>(), -1,
+                                  s, launches);
+                fft_lines<double>(d_buf.as<double2>(), m.ny + 1, tcc, (long)n1 * tcc, tcc, n0, m.nx + 1, p0,
+                                  tw0.as<double2>(), -1, s, launches);
+                long n = (long)(m.nx + 1) * (m.ny + 1) * tcc;
+                k_extract<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_buf.as<double2>(), m.nx, m.ny, tcc, Bs,
+                                                                      offs[c] + t0, quad.as<double2>());
+                EGX_CUDA(cudaGetLastError());
+                if (launches) *launches += 2;
+            }
+            EGX_CUDA(cudaStreamSynchronize(s));
+            if (stats) stats->ms_integrate += ms_since(t_int);
+        }
+    }
+    (void)t_start;
+}
+
+}  // namespace egx

@@ -283,6 +283,23 @@ void fft2d(C<T> *buf, int n0, int n1, int howmany, int sign, const C<T> *tw0, co
     if (launches) *launches += 2;
 }
 
+template <typename T>
+void fft_lines(C<T> *buf, int nlines, long lstride, long estride, int B, int nload, int nstore, const FftPlan &p,
+               const C<T> *tw, int sign, cudaStream_t s, long *launches) {
+    int bt = fft_cols(p.n, sizeof(C<T>));
+    size_t sm = 2 * (size_t)p.n * bt * sizeof(C<T>);
+    set_smem<T>((const void *)k_lines<T>, sm);
+    dim3 grid(nlines, (B + bt - 1) / bt);
+    k_lines<T><<<grid, threads_for(p.n * bt / 2), sm, s>>>(buf, lstride, estride, B, nload, nstore, p, tw, bt, sign);
+    EGX_CUDA(cudaGetLastError());
+    if (launches) *launches += 1;
+}
+
+template void fft_lines<double>(C<double> *, int, long, long, int, int, int, const FftPlan &, const C<double> *, int,
+                                cudaStream_t, long *);
+template void fft_lines<float>(C<float> *, int, long, long, int, int, int, const FftPlan &, const C<float> *, int,
+                               cudaStream_t, long *);
+
 std::vector<double> twiddles(int n) {
     std::vector<double> t(2 * (size_t)n);
     for (int m = 0; m < n; m++) {

@@ -41,6 +41,13 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
                     const C<T> *tw0, const C<T> *tw1, const FftPlan &p0, const FftPlan &p1, cudaStream_t s,
                     long *launches);
 
+// DFTs of `nlines` interleaved sequences: element e of line L, column b at
+// L*lstride + e*estride + b (b < B); elements e >= nload read as zero and
+// only e < nstore are written back.
+template <typename T>
+void fft_lines(C<T> *buf, int nlines, long lstride, long estride, int B, int nload, int nstore, const FftPlan &p,
+               const C<T> *tw, int sign, cudaStream_t s, long *launches);
+
 // In-place batched 2-D DFT (egx_fft2d).
 template <typename T>
 void fft2d(C<T> *buf, int n0, int n1, int howmany, int sign, const C<T> *tw0, const C<T> *tw1, const FftPlan &p0,
