@@ -1,92 +1,53 @@
-// extern "C" entry points of libegx.so (declared in include/egx.h).
-#include <complex>
+// extern "C" entry points of libegx.so (declared in include/egx.h): context,
+// Green tensor handles, operator, FFT, solvers, profiling.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
 #include <cstring>
-#include <map>
-#include <memory>
 
-#include "egx_green.cuh"
-#include "egx_krylov.cuh"
-#include "egx_operator.cuh"
+#include "egx_ctx.cuh"
 
 using namespace egx;
 typedef std::complex<double> cd;
 
-struct egx_green {
-    int nx = 0, ny = 0, nz = 0;
-    DevBuf g64;  // quadrant, complex128
-    DevBuf g32;  // quadrant, complex64 (mixed precision)
-    bool has32 = false;
-};
-
-struct egx_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    std::string err;
-    long launches = 0;
-
-    // prepared operator
-    egx_green *g = nullptr;
-    int type = -1;
-    int nx = 0, ny = 0, nz = 0;
-    DevBuf r64, fwd64, bwd64, r32, fwd32, bwd32;
-    bool prepared32 = false;
-    DevBuf buf64, buf32;
-    // FFT twiddles for the operator sizes
-    int tw_n0 = 0, tw_n1 = 0;
-    DevBuf tw0_64, tw1_64, tw0_32, tw1_32;
-    FftPlan p0{}, p1{};
-    // host staging
-    DevBuf xin, yout, xin32, yout32;
-    // solvers (cached workspaces)
-    std::unique_ptr<Gmres<double>> outer64, inner64;
-    std::unique_ptr<Gmres<float>> outer32, inner32;
-    std::string key64, key32;
-    // preconditioner plug
-    int precond_kind = EGX_PRECOND_GMRES;
-    egx_precond_fn precond_fn = nullptr;
-    void *precond_user = nullptr;
-    // FFT scratch for egx_fft2d
-    DevBuf fftbuf;
-    // mixed-solve workspace
-    DevBuf nrm_part, nrm_out, mix_r, mix_t, mix_r32, mix_d32;
-    std::map<int, std::pair<std::shared_ptr<DevBuf>, FftPlan>> tw_cache;
-    GreenBuildStats last_build;
-};
-
-namespace {
+namespace egx {
 
 int fail(egx_ctx *ctx, int code, const std::string &msg) {
     if (ctx) ctx->err = msg;
     return code;
 }
 
-#define EGX_GUARD(ctx, ...)                                             \
-    try {                                                               \
-        __VA_ARGS__;                                                    \
-        return EGX_OK;                                                  \
-    } catch (const egx::Error &e) {                                     \
-        return fail((ctx), e.code, e.what());                           \
-    } catch (const std::exception &e) {                                 \
-        return fail((ctx), EGX_ERR_INVALID, e.what());                  \
-    }
-
 void set_device(egx_ctx *ctx) { EGX_CUDA(cudaSetDevice(ctx->device)); }
 
-// Device copy of the twiddle table for length n in precision T.
+void check_device_error(egx_ctx *ctx) {
+    int flag = 0;
+    EGX_CUDA(cudaMemcpyAsync(&flag, ctx->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (flag) {
+        EGX_CUDA(cudaMemsetAsync(ctx->errflag.p, 0, sizeof(int), ctx->stream));
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        throw Error(flag, "a device wait timed out (shared-memory pipeline did not complete)");
+    }
+}
+
+long nvec(const egx_ctx *ctx) { return (long)ctx->nx * ctx->ny * 3 * ctx->nz; }
+
+namespace {
+
 template <typename T>
 void upload_twiddles(DevBuf &dst, int n, cudaStream_t s) {
     std::vector<double> t = twiddles(n);
     if (sizeof(T) == sizeof(double)) {
         dst.ensure(t.size() * sizeof(double));
         EGX_CUDA(cudaMemcpyAsync(dst.p, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, s));
-        EGX_CUDA(cudaStreamSynchronize(s));
     } else {
         std::vector<float> f(t.begin(), t.end());
         dst.ensure(f.size() * sizeof(float));
         EGX_CUDA(cudaMemcpyAsync(dst.p, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice, s));
         EGX_CUDA(cudaStreamSynchronize(s));
+        return;
     }
+    EGX_CUDA(cudaStreamSynchronize(s));
 }
 
 void ensure_twiddles(egx_ctx *ctx, int n0, int n1) {
@@ -101,7 +62,164 @@ void ensure_twiddles(egx_ctx *ctx, int n0, int n1) {
     ctx->tw_n1 = n1;
 }
 
-long nvec(const egx_ctx *ctx) { return (long)ctx->nx * ctx->ny * 3 * ctx->nz; }
+// r = (zeta - zeta0)/(zeta + conj zeta0) (A) or sqrt(Re zeta0)/(zeta + conj zeta0)
+// (Chi0) (ConvolutionOperator.PrepareRFunction, ConvolutionOperator.cs:113-143).
+__global__ void k_prepare_r(const double2 *__restrict__ zeta, const double2 *__restrict__ zeta0, int nz, long ncell,
+                            int type, double2 *__restrict__ r64, float2 *__restrict__ r32) {
+    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ncell * nz) return;
+    int k = (int)(idx % nz);
+    double2 z = zeta[idx], z0 = zeta0[k];
+    double2 den = make_double2(z.x + z0.x, z.y - z0.y);
+    double2 num = type == EGX_OP_CHI0 ? make_double2(sqrt(z0.x), 0.0) : make_double2(z.x - z0.x, z.y - z0.y);
+    double2 r = cdiv<double>(num, den);
+    r64[idx] = r;
+    if (r32) r32[idx] = make_float2((float)r.x, (float)r.y);
+}
+
+void gather_quadrant(int nx, int ny, int nz, const double *const comps[6], std::vector<cd> &q) {
+    GreenDims gd{nx, ny, nz};
+    const int S = gd.S(), A = gd.A(), Bs = gd.Bs(), lda = gd.lda();
+    q.assign((size_t)gd.Q() * Bs, cd(0, 0));
+    const int ref_blk[6] = {S, S, S, S, nz * nz, nz * nz};
+    const int off[6] = {0, S, 2 * S, 3 * S, 4 * S, 4 * S + A};
+    for (int a = 0; a <= nx; a++)
+        for (int b = 0; b <= ny; b++) {
+            long qi = (long)a * (ny + 1) + b;
+            long pt = (long)a * 2 * ny + b;
+            for (int c = 0; c < 6; c++) {
+                const cd *src = reinterpret_cast<const cd *>(comps[c]) + pt * ref_blk[c];
+                if (c < 4) {
+                    std::memcpy(&q[qi * Bs + off[c]], src, sizeof(cd) * S);
+                } else {
+                    for (int rc = 0; rc < nz; rc++)
+                        std::memcpy(&q[qi * Bs + off[c] + rc * lda], src + rc * nz, sizeof(cd) * nz);
+                }
+            }
+        }
+}
+
+template <typename T>
+GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in, double tol, int max_restarts,
+                       bool check_true, int precond_kind, int *n_applies) {
+    const long n = nvec(ctx);
+    const bool dbl = sizeof(T) == sizeof(double);
+    char keybuf[160];
+    snprintf(keybuf, sizeof keybuf, "%ld/%d/%d/%d/%d/%d", n, m_out, m_in, max_restarts, (int)check_true,
+             precond_kind);
+    std::unique_ptr<Gmres<T>> *outer, *inner;
+    std::string *key;
+    if (dbl) {
+        outer = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->outer64);
+        inner = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->inner64);
+        key = &ctx->key64;
+    } else {
+        outer = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->outer32);
+        inner = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->inner32);
+        key = &ctx->key32;
+    }
+    if (*key != keybuf) {
+        if (*outer) ctx->launches += (*outer)->kernel_launches;
+        if (*inner) ctx->launches += (*inner)->kernel_launches;
+        outer->reset();
+        inner->reset();
+        outer->reset(new Gmres<T>(n, m_out, tol, max_restarts, check_true, ctx->stream));
+        if (precond_kind == EGX_PRECOND_GMRES) inner->reset(new Gmres<T>(n, m_in, tol, 1, false, ctx->stream));
+        *key = keybuf;
+    }
+    // the inner GMRES runs one cycle to the outer tolerance
+    // (FlexibleGmresWithGmresPreconditioner.cs:35-44)
+    (*outer)->set_tol(tol);
+    if (*inner) (*inner)->set_tol(tol);
+    int applies = 0;
+    auto apply = [ctx, &applies](const C<T> *in, C<T> *out) {
+        apply_dev<T>(ctx, in, out, 1);
+        applies++;
+    };
+    (*outer)->apply = apply;
+    (*outer)->timers = &ctx->timers;
+    if (precond_kind == EGX_PRECOND_GMRES) {
+        (*inner)->apply = apply;
+        (*inner)->timers = &ctx->timers;
+        Gmres<T> *in = inner->get();
+        (*outer)->precond = [in](const C<T> *src, C<T> *dst) { in->solve(src, src, dst); };
+    } else if (precond_kind == EGX_PRECOND_CALLBACK) {
+        egx_precond_fn fn = ctx->precond_fn;
+        void *user = ctx->precond_user;
+        cudaStream_t s = ctx->stream;
+        const int prec = dbl ? EGX_PREC_FP64 : EGX_PREC_MIXED;
+        (*outer)->precond = [fn, user, n, s, prec](const C<T> *src, C<T> *dst) {
+            EGX_CUDA(cudaStreamSynchronize(s));
+            int rc = fn(user, src, dst, n, prec);
+            if (rc != 0) throw Error(EGX_ERR_INVALID, "preconditioner callback failed");
+        };
+    } else {
+        (*outer)->precond = nullptr;
+    }
+    GmresResult r = (*outer)->solve(b, x, x);
+    *n_applies = applies;
+    return r;
+}
+
+}  // namespace
+
+void upload_model(egx_ctx *ctx, egx_green *g, const double *zeta, const double *zeta0, int where) {
+    const long ncell = (long)g->nx * g->ny;
+    ctx->zeta.ensure(ncell * g->nz * sizeof(double2));
+    ctx->zeta0.ensure(g->nz * sizeof(double2));
+    cudaMemcpyKind kind = where == EGX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    EGX_CUDA(cudaMemcpyAsync(ctx->zeta.p, zeta, ncell * g->nz * sizeof(double2), kind, ctx->stream));
+    EGX_CUDA(cudaMemcpyAsync(ctx->zeta0.p, zeta0, g->nz * sizeof(double2), kind, ctx->stream));
+}
+
+void prepare_device(egx_ctx *ctx, egx_green *g, const double *dz, int type) {
+    EGX_CHECK(type == EGX_OP_A || type == EGX_OP_CHI0, EGX_ERR_INVALID, "unknown operator type");
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    std::vector<cd> z0(nz);
+    EGX_CUDA(cudaMemcpyAsync(z0.data(), ctx->zeta0.p, nz * sizeof(cd), cudaMemcpyDeviceToHost, ctx->stream));
+    EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+    // PrepareForwardFactors / PrepareBackwardFactors (ConvolutionOperator.cs:90-111)
+    std::vector<cd> fwd(nz), bwd(nz);
+    const cd norm(1.0 / ((double)nx * (double)ny * 4), 0);
+    for (int k = 0; k < nz; k++) {
+        EGX_CHECK(dz[k] > 0, EGX_ERR_INVALID, "layer thickness must be positive");
+        fwd[k] = cd(std::sqrt(z0[k].real()), 0);
+        cd sc(2 * std::sqrt(z0[k].real()), 0);
+        sc /= dz[k];
+        sc *= norm;
+        bwd[k] = sc;
+    }
+    const long ncell = (long)nx * ny;
+    ctx->r64.ensure(ncell * nz * sizeof(double2));
+    ctx->fwd64.ensure(nz * sizeof(double2));
+    ctx->bwd64.ensure(nz * sizeof(double2));
+    EGX_CUDA(cudaMemcpyAsync(ctx->fwd64.p, fwd.data(), nz * sizeof(cd), cudaMemcpyHostToDevice, ctx->stream));
+    EGX_CUDA(cudaMemcpyAsync(ctx->bwd64.p, bwd.data(), nz * sizeof(cd), cudaMemcpyHostToDevice, ctx->stream));
+    float2 *r32 = nullptr;
+    if (g->has32) {
+        ctx->r32.ensure(ncell * nz * sizeof(float2));
+        ctx->fwd32.ensure(nz * sizeof(float2));
+        ctx->bwd32.ensure(nz * sizeof(float2));
+        r32 = ctx->r32.as<float2>();
+    }
+    long n = ncell * nz;
+    k_prepare_r<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(ctx->zeta.as<double2>(), ctx->zeta0.as<double2>(),
+                                                                      nz, ncell, type, ctx->r64.as<double2>(), r32);
+    ctx->launches++;
+    if (g->has32) {
+        convert_d2f(ctx->fwd64.as<double2>(), ctx->fwd32.as<float2>(), nz, 1.0, ctx->stream);
+        convert_d2f(ctx->bwd64.as<double2>(), ctx->bwd32.as<float2>(), nz, 1.0, ctx->stream);
+        ctx->launches += 2;
+    }
+    EGX_CUDA(cudaGetLastError());
+    ctx->prepared32 = g->has32;
+    ensure_twiddles(ctx, 2 * nx, 2 * ny);
+    ctx->g = g;
+    ctx->type = type;
+    ctx->nx = nx;
+    ctx->ny = ny;
+    ctx->nz = nz;
+}
 
 template <typename T>
 void apply_dev(egx_ctx *ctx, const C<T> *x, C<T> *y, int nrhs) {
@@ -126,28 +244,111 @@ void apply_dev(egx_ctx *ctx, const C<T> *x, C<T> *y, int nrhs) {
     const C<T> *G = dbl ? (const C<T> *)ctx->g->g64.p : (const C<T> *)ctx->g->g32.p;
     const C<T> *tw0 = dbl ? (const C<T> *)ctx->tw0_64.p : (const C<T> *)ctx->tw0_32.p;
     const C<T> *tw1 = dbl ? (const C<T> *)ctx->tw1_64.p : (const C<T> *)ctx->tw1_32.p;
-    operator_apply<T>(d, op, G, x, y, buf.as<C<T>>(), tw0, tw1, ctx->p0, ctx->p1, ctx->stream, &ctx->launches);
+    operator_apply<T>(d, op, G, x, y, buf.as<C<T>>(), tw0, tw1, ctx->p0, ctx->p1, ctx->stream, &ctx->launches,
+                      &ctx->timers, ctx->errflag.as<int>());
+}
+template void apply_dev<double>(egx_ctx *, const C<double> *, C<double> *, int);
+template void apply_dev<float>(egx_ctx *, const C<float> *, C<float> *, int);
+
+GmresResult fgmres_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_gmres_params &p, int *applies) {
+    EGX_CHECK(p.m_out >= 1 && p.m_in >= 1 && p.max_restarts >= 1 && p.tol > 0, EGX_ERR_INVALID,
+              "bad GMRES parameters");
+    int kind = p.precond;
+    if (kind == EGX_PRECOND_GMRES && ctx->precond_kind == EGX_PRECOND_CALLBACK) kind = EGX_PRECOND_CALLBACK;
+    if (ctx->precond_kind == EGX_PRECOND_NONE) kind = EGX_PRECOND_NONE;
+    return run_fgmres<double>(ctx, b, x, p.m_out, p.m_in, p.tol, p.max_restarts, p.check_true != 0, kind, applies);
 }
 
-// Quadrant point (a, b) <- reference layout point (a, b).
-void gather_quadrant(int nx, int ny, int nz, const double *const comps[6], std::vector<cd> &q) {
-    GreenDims gd{nx, ny, nz};
-    const int S = gd.S(), A = gd.A(), Bs = gd.Bs();
-    q.assign((size_t)gd.Q() * Bs, cd(0, 0));
-    const int blk[6] = {S, S, S, S, A, A};
-    const int off[6] = {0, S, 2 * S, 3 * S, 4 * S, 4 * S + A};
-    for (int a = 0; a <= nx; a++)
-        for (int b = 0; b <= ny; b++) {
-            long qi = (long)a * (ny + 1) + b;
-            long pt = (long)a * 2 * ny + b;
-            for (int c = 0; c < 6; c++) {
-                const cd *src = reinterpret_cast<const cd *>(comps[c]) + pt * blk[c];
-                std::memcpy(&q[qi * Bs + off[c]], src, sizeof(cd) * blk[c]);
-            }
-        }
+// Outer FP64 iterative refinement: r = b - A x (complex128 apply), inner
+// complex64 FGMRES on A d = r/||r||, x += ||r|| d, until ||r||/||b|| < tol.
+// The inner relative tolerance of a refinement at true residual be is
+// max(inner_tol, min(0.5, kInnerSafety * tol / be)).
+static const double kInnerSafety = 0.3;
+GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixed_params &p, int *applies,
+                      int *refinements, double *true_be) {
+    EGX_CHECK(p.m_out >= 1 && p.m_in >= 1 && p.max_outer >= 1 && p.tol > 0 && p.inner_tol > 0 &&
+                  p.inner_restarts >= 1,
+              EGX_ERR_INVALID, "bad mixed-solve parameters");
+    EGX_CHECK(ctx->g->has32 && ctx->prepared32, EGX_ERR_STATE,
+              "mixed solve needs a Green tensor built or uploaded with EGX_PREC_MIXED");
+    const long n = nvec(ctx);
+    ctx->mix_r.ensure(n * sizeof(double2));
+    ctx->mix_t.ensure(n * sizeof(double2));
+    ctx->mix_r32.ensure(n * sizeof(float2));
+    ctx->mix_d32.ensure(n * sizeof(float2));
+    ctx->nrm_part.ensure(2048 * sizeof(double));
+    ctx->nrm_out.ensure(sizeof(double));
+    double2 *r = ctx->mix_r.as<double2>(), *t = ctx->mix_t.as<double2>();
+    float2 *r32 = ctx->mix_r32.as<float2>(), *d32 = ctx->mix_d32.as<float2>();
+    auto norm64 = [&](const double2 *v) {
+        VecOps<double>::norm2(v, n, ctx->nrm_out.as<double>(), ctx->nrm_part.as<double>(), 1024, ctx->stream);
+        ctx->launches += 2;
+        double h;
+        EGX_CUDA(cudaMemcpyAsync(&h, ctx->nrm_out.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        return std::sqrt(h);
+    };
+    int applies64 = 0, applies32 = 0;
+    GmresResult out;
+    double bn = norm64(b);
+    if (bn == 0) {
+        VecOps<double>::zero(x, n, ctx->stream);
+        out.converged = true;
+        *applies = 0;
+        *refinements = 0;
+        *true_be = 0;
+        return out;
+    }
+    apply_dev<double>(ctx, x, t, 1);
+    applies64++;
+    VecOps<double>::sub(b, t, r, n, ctx->stream);
+    ctx->launches++;
+    double rn = norm64(r);
+    double be = rn / bn;
+    int k = 0;
+    bool conv = be < p.tol;
+    while (!conv && k < p.max_outer) {
+        convert_d2f(r, r32, n, 1.0 / rn, ctx->stream);
+        VecOps<float>::zero(d32, n, ctx->stream);
+        ctx->launches += 1;
+        int a32 = 0;
+        // ask the inner solve only for the reduction still needed (with a
+        // safety factor), never for less than inner_tol
+        double itol = std::max(p.inner_tol, std::min(0.5, kInnerSafety * p.tol / be));
+        GmresResult ir = run_fgmres<float>(ctx, r32, d32, p.m_out, p.m_in, itol, p.inner_restarts, false,
+                                           EGX_PRECOND_GMRES, &a32);
+        applies32 += a32;
+        out.iterations += ir.iterations;
+        out.arnoldi_be = ir.arnoldi_be;
+        convert_f2d_add(d32, x, n, rn, ctx->stream);
+        apply_dev<double>(ctx, x, t, 1);
+        applies64++;
+        VecOps<double>::sub(b, t, r, n, ctx->stream);
+        ctx->launches += 2;
+        rn = norm64(r);
+        be = rn / bn;
+        k++;
+        conv = be < p.tol;
+    }
+    out.converged = conv;
+    out.true_be = be;
+    *applies = applies64 + applies32;
+    *refinements = k;
+    *true_be = be;
+    return out;
 }
 
-}  // namespace
+}  // namespace egx
+
+#define EGX_GUARD(ctx, ...)                                             \
+    try {                                                               \
+        __VA_ARGS__;                                                    \
+        return EGX_OK;                                                  \
+    } catch (const egx::Error &e) {                                     \
+        return fail((ctx), e.code, e.what());                           \
+    } catch (const std::exception &e) {                                 \
+        return fail((ctx), EGX_ERR_INVALID, e.what());                  \
+    }
 
 extern "C" {
 
@@ -162,6 +363,8 @@ int egx_create(int device, egx_ctx **out) {
         set_device(ctx);
         EGX_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
         ctx->own_stream = true;
+        ctx->errflag.ensure(sizeof(int));
+        EGX_CUDA(cudaMemset(ctx->errflag.p, 0, sizeof(int)));
     } catch (const egx::Error &e) {
         delete ctx;
         return e.code;
@@ -174,6 +377,7 @@ int egx_destroy(egx_ctx *ctx) {
     if (!ctx) return EGX_ERR_INVALID;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    ctx->timers.flush();
     ctx->outer64.reset();
     ctx->inner64.reset();
     ctx->outer32.reset();
@@ -195,6 +399,7 @@ int egx_set_stream(egx_ctx *ctx, void *stream) {
     EGX_GUARD(ctx, {
         set_device(ctx);
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->timers.flush();
         if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
         ctx->stream = (cudaStream_t)stream;
         ctx->own_stream = false;
@@ -215,6 +420,25 @@ long egx_launch_count(egx_ctx *ctx) {
     if (ctx->outer32) n += ctx->outer32->kernel_launches;
     if (ctx->inner32) n += ctx->inner32->kernel_launches;
     return n;
+}
+
+int egx_profile(egx_ctx *ctx, int enable) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        set_device(ctx);
+        ctx->timers.reset();
+        ctx->timers.on = enable != 0;
+    });
+}
+
+int egx_profile_read(egx_ctx *ctx, int kind, long *launches, double *total_ms) {
+    if (!ctx || !launches || !total_ms || kind < 0 || kind >= Timers::kKinds) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        set_device(ctx);
+        ctx->timers.flush();
+        *launches = ctx->timers.count[kind];
+        *total_ms = ctx->timers.total_ms[kind];
+    });
 }
 
 int egx_green_build(egx_ctx *ctx, const egx_model *model, double omega, int n_hankels, int precision,
@@ -243,7 +467,7 @@ int egx_green_build(egx_ctx *ctx, const egx_model *model, double omega, int n_ha
         g->ny = gm.ny;
         g->nz = gm.nz;
         GreenBuildStats st;
-        build_green(gm, n_hankels, ctx->stream, g->g64, &st, &ctx->launches);
+        build_green(gm, n_hankels, ctx->stream, g->g64, &st, &ctx->launches, &ctx->timers);
         if (precision == EGX_PREC_MIXED) {
             GreenDims gd{gm.nx, gm.ny, gm.nz};
             long n = gd.Q() * gd.Bs();
@@ -290,11 +514,11 @@ int egx_green_download(egx_ctx *ctx, const egx_green *g, double *const comps[6])
         EGX_CHECK(g && comps, EGX_ERR_INVALID, "bad arguments");
         set_device(ctx);
         GreenDims gd{g->nx, g->ny, g->nz};
-        const int S = gd.S(), A = gd.A(), Bs = gd.Bs();
+        const int S = gd.S(), A = gd.A(), Bs = gd.Bs(), lda = gd.lda(), nz = g->nz;
         std::vector<cd> q((size_t)gd.Q() * Bs);
         EGX_CUDA(cudaMemcpyAsync(q.data(), g->g64.p, q.size() * sizeof(cd), cudaMemcpyDeviceToHost, ctx->stream));
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));
-        const int blk[6] = {S, S, S, S, A, A};
+        const int blk[6] = {S, S, S, S, nz * nz, nz * nz};
         const int off[6] = {0, S, 2 * S, 3 * S, 4 * S, 4 * S + A};
         // parity (x, y) of xx, xy, yy, zz, xz, yz
         const int px[6] = {1, -1, 1, 1, -1, 1}, py[6] = {1, -1, 1, 1, 1, -1};
@@ -310,7 +534,12 @@ int egx_green_download(egx_ctx *ctx, const egx_green *g, double *const comps[6])
                     double sg = (mx ? px[c] : 1) * (my ? py[c] : 1);
                     cd *dst = reinterpret_cast<cd *>(comps[c]) + pt * blk[c];
                     const cd *src = &q[qi * Bs + off[c]];
-                    for (int t = 0; t < blk[c]; t++) dst[t] = sg * src[t];
+                    if (c < 4) {
+                        for (int t = 0; t < blk[c]; t++) dst[t] = sg * src[t];
+                    } else {
+                        for (int rc = 0; rc < nz; rc++)
+                            for (int tr = 0; tr < nz; tr++) dst[rc * nz + tr] = sg * src[rc * lda + tr];
+                    }
                 }
             }
     });
@@ -333,52 +562,10 @@ int egx_op_prepare(egx_ctx *ctx, egx_green *g, const double *zeta, const double 
     EGX_GUARD(ctx, {
         EGX_CHECK(g, EGX_ERR_INVALID, "greenTensor is null");
         EGX_CHECK(zeta && zeta0 && dz, EGX_ERR_INVALID, "null model arrays");
-        EGX_CHECK(type == EGX_OP_A || type == EGX_OP_CHI0, EGX_ERR_INVALID, "unknown operator type");
         set_device(ctx);
-        const int nx = g->nx, ny = g->ny, nz = g->nz;
-        const cd *z = reinterpret_cast<const cd *>(zeta);
-        const cd *z0 = reinterpret_cast<const cd *>(zeta0);
-        // PrepareRFunction / PrepareForwardFactors / PrepareBackwardFactors (ConvolutionOperator.cs:90-143)
-        std::vector<cd> r((size_t)nx * ny * nz), fwd(nz), bwd(nz);
-        const cd norm(1.0 / ((double)nx * (double)ny * 4), 0);
-        for (int k = 0; k < nz; k++) {
-            fwd[k] = cd(std::sqrt(z0[k].real()), 0);
-            cd sc(2 * std::sqrt(z0[k].real()), 0);
-            sc /= dz[k];
-            sc *= norm;
-            bwd[k] = sc;
-        }
-        for (long i = 0; i < (long)nx * ny; i++)
-            for (int k = 0; k < nz; k++) {
-                cd zz = z[i * nz + k];
-                cd conj0 = std::conj(z0[k]);
-                if (type == EGX_OP_CHI0) r[i * nz + k] = cd(std::sqrt(z0[k].real()), 0) / (zz + conj0);
-                else r[i * nz + k] = (zz - z0[k]) / (zz + conj0);
-            }
-        ctx->r64.ensure(r.size() * sizeof(cd));
-        ctx->fwd64.ensure(nz * sizeof(cd));
-        ctx->bwd64.ensure(nz * sizeof(cd));
-        EGX_CUDA(cudaMemcpyAsync(ctx->r64.p, r.data(), r.size() * sizeof(cd), cudaMemcpyHostToDevice, ctx->stream));
-        EGX_CUDA(cudaMemcpyAsync(ctx->fwd64.p, fwd.data(), nz * sizeof(cd), cudaMemcpyHostToDevice, ctx->stream));
-        EGX_CUDA(cudaMemcpyAsync(ctx->bwd64.p, bwd.data(), nz * sizeof(cd), cudaMemcpyHostToDevice, ctx->stream));
-        ctx->prepared32 = false;
-        if (g->has32) {
-            ctx->r32.ensure(r.size() * sizeof(float2));
-            ctx->fwd32.ensure(nz * sizeof(float2));
-            ctx->bwd32.ensure(nz * sizeof(float2));
-            convert_d2f(ctx->r64.as<double2>(), ctx->r32.as<float2>(), (long)r.size(), 1.0, ctx->stream);
-            convert_d2f(ctx->fwd64.as<double2>(), ctx->fwd32.as<float2>(), nz, 1.0, ctx->stream);
-            convert_d2f(ctx->bwd64.as<double2>(), ctx->bwd32.as<float2>(), nz, 1.0, ctx->stream);
-            ctx->launches += 3;
-            ctx->prepared32 = true;
-        }
-        ensure_twiddles(ctx, 2 * nx, 2 * ny);
+        upload_model(ctx, g, zeta, zeta0, EGX_HOST);
+        prepare_device(ctx, g, dz, type);
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));
-        ctx->g = g;
-        ctx->type = type;
-        ctx->nx = nx;
-        ctx->ny = ny;
-        ctx->nz = nz;
     });
 }
 
@@ -399,6 +586,7 @@ int egx_op_apply(egx_ctx *ctx, const double *x, double *y, int nrhs, int where) 
             EGX_CUDA(cudaMemcpyAsync(y, ctx->yout.p, n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
         }
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        check_device_error(ctx);
     });
 }
 
@@ -419,6 +607,7 @@ int egx_op_apply_c64(egx_ctx *ctx, const float *x, float *y, int nrhs, int where
             EGX_CUDA(cudaMemcpyAsync(y, ctx->yout32.p, n * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream));
         }
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        check_device_error(ctx);
     });
 }
 
@@ -460,79 +649,12 @@ int egx_set_precond(egx_ctx *ctx, int kind, egx_precond_fn fn, void *user) {
     return EGX_OK;
 }
 
-}  // extern "C"
-
-namespace {
-
-// FGMRES with the inner GMRES preconditioner (or a callback / none) in
-// precision T on device vectors b, x (x holds the initial guess).
-template <typename T>
-GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in, double tol, int max_restarts,
-                       bool check_true, int precond_kind, int *n_applies, bool zero_guess_inner_rhs) {
-    const long n = nvec(ctx);
-    const bool dbl = sizeof(T) == sizeof(double);
-    char keybuf[128];
-    snprintf(keybuf, sizeof keybuf, "%ld/%d/%d/%g/%d/%d/%d", n, m_out, m_in, tol, max_restarts, (int)check_true,
-             precond_kind);
-    std::unique_ptr<Gmres<T>> *outer, *inner;
-    std::string *key;
-    if (dbl) {
-        outer = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->outer64);
-        inner = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->inner64);
-        key = &ctx->key64;
-    } else {
-        outer = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->outer32);
-        inner = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->inner32);
-        key = &ctx->key32;
-    }
-    if (*key != keybuf) {
-        outer->reset();
-        inner->reset();
-        outer->reset(new Gmres<T>(n, m_out, tol, max_restarts, check_true, ctx->stream));
-        if (precond_kind == EGX_PRECOND_GMRES) inner->reset(new Gmres<T>(n, m_in, tol, 1, false, ctx->stream));
-        *key = keybuf;
-    }
-    int applies = 0;
-    auto apply = [ctx, &applies](const C<T> *in, C<T> *out) {
-        apply_dev<T>(ctx, in, out, 1);
-        applies++;
-    };
-    (*outer)->apply = apply;
-    if (precond_kind == EGX_PRECOND_GMRES) {
-        (*inner)->apply = apply;
-        Gmres<T> *in = inner->get();
-        (*outer)->precond = [in](const C<T> *src, C<T> *dst) { in->solve(src, src, dst); };
-    } else if (precond_kind == EGX_PRECOND_CALLBACK) {
-        egx_precond_fn fn = ctx->precond_fn;
-        void *user = ctx->precond_user;
-        cudaStream_t s = ctx->stream;
-        const int prec = dbl ? EGX_PREC_FP64 : EGX_PREC_MIXED;
-        (*outer)->precond = [fn, user, n, s, prec](const C<T> *src, C<T> *dst) {
-            EGX_CUDA(cudaStreamSynchronize(s));
-            int rc = fn(user, src, dst, n, prec);
-            if (rc != 0) throw Error(EGX_ERR_INVALID, "preconditioner callback failed");
-        };
-    } else {
-        (*outer)->precond = nullptr;
-    }
-    (void)zero_guess_inner_rhs;
-    GmresResult r = (*outer)->solve(b, x, x);
-    *n_applies = applies;
-    return r;
-}
-
-}  // namespace
-
-extern "C" {
-
 int egx_fgmres_solve(egx_ctx *ctx, const double *b, double *x, const egx_gmres_params *p, egx_result *res,
                      int where) {
     if (!ctx) return EGX_ERR_INVALID;
     int status = EGX_OK;
     try {
         EGX_CHECK(b && x && p && res, EGX_ERR_INVALID, "bad solve arguments");
-        EGX_CHECK(p->m_out >= 1 && p->m_in >= 1 && p->max_restarts >= 1 && p->tol > 0, EGX_ERR_INVALID,
-                  "bad GMRES parameters");
         set_device(ctx);
         EGX_CHECK(ctx->g && ctx->type >= 0, EGX_ERR_STATE, "operator is not prepared");
         const long n = nvec(ctx);
@@ -548,14 +670,12 @@ int egx_fgmres_solve(egx_ctx *ctx, const double *b, double *x, const egx_gmres_p
             EGX_CUDA(cudaMemcpyAsync((void *)db, b, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
             EGX_CUDA(cudaMemcpyAsync(dx, x, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
         }
-        int kind = p->precond;
-        if (kind == EGX_PRECOND_GMRES && ctx->precond_kind == EGX_PRECOND_CALLBACK) kind = EGX_PRECOND_CALLBACK;
         int applies = 0;
-        GmresResult r = run_fgmres<double>(ctx, db, dx, p->m_out, p->m_in, p->tol, p->max_restarts,
-                                           p->check_true != 0, kind, &applies, false);
+        GmresResult r = fgmres_dev(ctx, db, dx, *p, &applies);
         if (where != EGX_DEVICE)
             EGX_CUDA(cudaMemcpyAsync(x, dx, n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        check_device_error(ctx);
         res->converged = r.converged;
         res->iterations = r.iterations;
         res->arnoldi_be = r.arnoldi_be;
@@ -577,12 +697,8 @@ int egx_mixed_solve(egx_ctx *ctx, const double *b, double *x, const egx_mixed_pa
     int status = EGX_OK;
     try {
         EGX_CHECK(b && x && p && res, EGX_ERR_INVALID, "bad solve arguments");
-        EGX_CHECK(p->m_out >= 1 && p->m_in >= 1 && p->max_outer >= 1 && p->tol > 0 && p->inner_tol > 0,
-                  EGX_ERR_INVALID, "bad mixed-solve parameters");
         set_device(ctx);
         EGX_CHECK(ctx->g && ctx->type >= 0, EGX_ERR_STATE, "operator is not prepared");
-        EGX_CHECK(ctx->g->has32 && ctx->prepared32, EGX_ERR_STATE,
-                  "mixed solve needs a Green tensor built or uploaded with EGX_PREC_MIXED");
         const long n = nvec(ctx);
         const double2 *db;
         double2 *dx;
@@ -596,72 +712,58 @@ int egx_mixed_solve(egx_ctx *ctx, const double *b, double *x, const egx_mixed_pa
             EGX_CUDA(cudaMemcpyAsync((void *)db, b, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
             EGX_CUDA(cudaMemcpyAsync(dx, x, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
         }
-        // outer FP64 iterative refinement: r = b - A x (FP64), inner complex64
-        // FGMRES on A d = r / ||r||, x += ||r|| d.
-        DevBuf &r32 = ctx->mix_r32, &d32 = ctx->mix_d32;
-        ctx->mix_r.ensure(n * sizeof(double2));
-        ctx->mix_t.ensure(n * sizeof(double2));
-        r32.ensure(n * sizeof(float2));
-        d32.ensure(n * sizeof(float2));
-        ctx->nrm_part.ensure(2048 * sizeof(double));
-        ctx->nrm_out.ensure(sizeof(double));
-        double2 *r = ctx->mix_r.as<double2>(), *t = ctx->mix_t.as<double2>();
-        int applies64 = 0, applies32 = 0, iters = 0;
-        auto norm64 = [&](const double2 *v) {
-            DevBuf &out = ctx->nrm_out;
-            VecOps<double>::norm2(v, n, out.as<double>(), ctx->nrm_part.as<double>(), 1024, ctx->stream);
-            ctx->launches += 2;
-            double h;
-            EGX_CUDA(cudaMemcpyAsync(&h, out.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-            EGX_CUDA(cudaStreamSynchronize(ctx->stream));
-            return std::sqrt(h);
-        };
-        double bn = norm64(db);
-        apply_dev<double>(ctx, dx, t, 1);
-        applies64++;
-        VecOps<double>::sub(db, t, r, n, ctx->stream);
-        ctx->launches++;
-        double rn = norm64(r);
-        double be = bn > 0 ? rn / bn : 0.0;
-        int k = 0;
-        bool conv = be < p->tol;
-        double last_arnoldi = -1;
-        while (!conv && k < p->max_outer) {
-            convert_d2f(r, r32.as<float2>(), n, 1.0 / rn, ctx->stream);
-            VecOps<float>::zero(d32.as<float2>(), n, ctx->stream);
-            ctx->launches += 1;
-            int a32 = 0;
-            GmresResult ir = run_fgmres<float>(ctx, r32.as<float2>(), d32.as<float2>(), p->m_out, p->m_in,
-                                               p->inner_tol, p->inner_restarts, false, EGX_PRECOND_GMRES, &a32, true);
-            applies32 += a32;
-            iters += ir.iterations;
-            last_arnoldi = ir.arnoldi_be;
-            convert_f2d_add(d32.as<float2>(), dx, n, rn, ctx->stream);
-            apply_dev<double>(ctx, dx, t, 1);
-            applies64++;
-            VecOps<double>::sub(db, t, r, n, ctx->stream);
-            ctx->launches += 2;
-            rn = norm64(r);
-            be = rn / bn;
-            k++;
-            conv = be < p->tol;
-        }
+        int applies = 0, refinements = 0;
+        double tbe = -1;
+        GmresResult r = mixed_dev(ctx, db, dx, *p, &applies, &refinements, &tbe);
         if (where != EGX_DEVICE)
             EGX_CUDA(cudaMemcpyAsync(x, dx, n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));
-        res->converged = conv;
-        res->iterations = iters;
-        res->arnoldi_be = last_arnoldi;
-        res->true_be = be;
-        res->n_applies = applies64 + applies32;
-        res->n_refinements = k;
-        if (!conv) status = fail(ctx, EGX_ERR_NOT_CONVERGED, "mixed-precision refinement did not converge");
+        check_device_error(ctx);
+        res->converged = r.converged;
+        res->iterations = r.iterations;
+        res->arnoldi_be = r.arnoldi_be;
+        res->true_be = tbe;
+        res->n_applies = applies;
+        res->n_refinements = refinements;
+        if (!r.converged) status = fail(ctx, EGX_ERR_NOT_CONVERGED, "mixed-precision refinement did not converge");
     } catch (const egx::Error &e) {
         return fail(ctx, e.code, e.what());
     } catch (const std::exception &e) {
         return fail(ctx, EGX_ERR_INVALID, e.what());
     }
     return status;
+}
+
+int egx_dot_products(egx_ctx *ctx, const double *V, int ncols, const double *w, long n, double *out, int where) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(V && w && out && ncols >= 1 && ncols <= 64 && n >= 1, EGX_ERR_INVALID,
+                  "bad dot-product arguments");
+        set_device(ctx);
+        const double2 *dV, *dw;
+        if (where == EGX_DEVICE) {
+            dV = (const double2 *)V;
+            dw = (const double2 *)w;
+        } else {
+            ctx->xin.ensure((size_t)(ncols + 1) * n * sizeof(double2));
+            double2 *stage = ctx->xin.as<double2>();
+            EGX_CUDA(cudaMemcpyAsync(stage, V, (size_t)ncols * n * sizeof(double2), cudaMemcpyHostToDevice,
+                                     ctx->stream));
+            EGX_CUDA(cudaMemcpyAsync(stage + (size_t)ncols * n, w, n * sizeof(double2), cudaMemcpyHostToDevice,
+                                     ctx->stream));
+            dV = stage;
+            dw = stage + (size_t)ncols * n;
+        }
+        int nblocks = (int)std::min<long>(1024, (n + 255) / 256);
+        ctx->nrm_part.ensure((size_t)nblocks * 64 * sizeof(double2));
+        ctx->yout.ensure(64 * sizeof(double2));
+        VecOps<double>::multi_dot(dV, ncols, dw, n, ctx->yout.as<double2>(), ctx->nrm_part.as<double2>(), nblocks,
+                                  ctx->stream);
+        ctx->launches += 2;
+        cudaMemcpyKind k = where == EGX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        EGX_CUDA(cudaMemcpyAsync(out, ctx->yout.p, ncols * sizeof(double2), k, ctx->stream));
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
 }
 
 }  // extern "C"

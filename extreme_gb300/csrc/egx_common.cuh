@@ -71,6 +71,72 @@ struct Error : std::runtime_error {
         if (!(cond)) throw ::egx::Error((code), (msg));                                \
     } while (0)
 
+// Per-kernel device time, measured with CUDA events recorded on the launch
+// stream around each launch of an instrumented kernel (enabled on demand).
+struct Timers {
+    static const int kKinds = 32;
+    bool on = false;
+    struct Rec {
+        int kind;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    double total_ms[kKinds] = {};
+    long count[kKinds] = {};
+    cudaEvent_t take() {
+        if (pool.empty()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            return e;
+        }
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    // returns the record index to close with end()
+    int begin(int kind, cudaStream_t s) {
+        if (!on) return -1;
+        Rec r{kind, take(), take()};
+        cudaEventRecord(r.a, s);
+        pending.push_back(r);
+        return (int)pending.size() - 1;
+    }
+    void end(int idx, cudaStream_t s) {
+        if (idx < 0) return;
+        cudaEventRecord(pending[idx].b, s);
+        if (pending.size() > 4000) flush();
+    }
+    void flush() {
+        for (auto &r : pending) {
+            cudaEventSynchronize(r.b);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, r.a, r.b);
+            if (r.kind >= 0 && r.kind < kKinds) {
+                total_ms[r.kind] += ms;
+                count[r.kind]++;
+            }
+            pool.push_back(r.a);
+            pool.push_back(r.b);
+        }
+        pending.clear();
+    }
+    void reset() {
+        flush();
+        for (int k = 0; k < kKinds; k++) {
+            total_ms[k] = 0;
+            count[k] = 0;
+        }
+    }
+    ~Timers() {
+        for (auto &r : pending) {
+            cudaEventDestroy(r.a);
+            cudaEventDestroy(r.b);
+        }
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+
 // Device buffer owned by the context.
 struct DevBuf {
     void *p = nullptr;

@@ -1,0 +1,75 @@
+// The egx_ctx / egx_green objects behind the C ABI and the per-kernel timers.
+#pragma once
+
+#include <complex>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "egx_green.cuh"
+#include "egx_krylov.cuh"
+#include "egx_operator.cuh"
+
+struct egx_green {
+    int nx = 0, ny = 0, nz = 0;
+    egx::DevBuf g64;  // quadrant, complex128
+    egx::DevBuf g32;  // quadrant, complex64 (mixed precision)
+    bool has32 = false;
+};
+
+struct egx_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    long launches = 0;
+    egx::Timers timers;
+
+    // prepared operator
+    egx_green *g = nullptr;
+    int type = -1;
+    int nx = 0, ny = 0, nz = 0;
+    egx::DevBuf zeta, zeta0;                 // device copies of the model (complex128)
+    egx::DevBuf r64, fwd64, bwd64, r32, fwd32, bwd32;
+    bool prepared32 = false;
+    egx::DevBuf buf64, buf32;
+    int tw_n0 = 0, tw_n1 = 0;
+    egx::DevBuf tw0_64, tw1_64, tw0_32, tw1_32;
+    egx::FftPlan p0{}, p1{};
+    // host staging
+    egx::DevBuf xin, yout, xin32, yout32, src_io;
+    // solvers (cached workspaces)
+    std::unique_ptr<egx::Gmres<double>> outer64, inner64;
+    std::unique_ptr<egx::Gmres<float>> outer32, inner32;
+    std::string key64, key32;
+    // preconditioner plug
+    int precond_kind = EGX_PRECOND_GMRES;
+    egx_precond_fn precond_fn = nullptr;
+    void *precond_user = nullptr;
+    egx::DevBuf fftbuf;
+    egx::DevBuf nrm_part, nrm_out, mix_r, mix_t, mix_r32, mix_d32;
+    egx::DevBuf js, chi0;
+    egx::DevBuf errflag;  // device int: EGX_ERR_TIMEOUT from a bounded wait
+    egx::GreenBuildStats last_build;
+};
+
+namespace egx {
+
+// Operator/solver helpers shared by egx_api.cu and egx_mt.cu.
+void set_device(egx_ctx *ctx);
+long nvec(const egx_ctx *ctx);
+// PrepareOperator from the device copies of zeta/zeta0 already held in ctx.
+void prepare_device(egx_ctx *ctx, egx_green *g, const double *dz_host, int type);
+// Upload zeta [nx][ny][nz] and zeta0 [nz] (host or device pointers).
+void upload_model(egx_ctx *ctx, egx_green *g, const double *zeta, const double *zeta0, int where);
+template <typename T> void apply_dev(egx_ctx *ctx, const C<T> *x, C<T> *y, int nrhs);
+GmresResult fgmres_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_gmres_params &p, int *applies);
+GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixed_params &p, int *applies,
+                      int *refinements, double *true_be);
+int fail(egx_ctx *ctx, int code, const std::string &msg);
+// Throws EGX_ERR_TIMEOUT (and clears the flag) if a kernel gave up a bounded
+// wait; call after a stream synchronisation.
+void check_device_error(egx_ctx *ctx);
+
+}  // namespace egx

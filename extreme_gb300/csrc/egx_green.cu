@@ -372,15 +372,19 @@ __global__ void k_cells(const int *__restrict__ rowptr, const Term *__restrict__
     }
 }
 
-__global__ void k_extract(const double2 *__restrict__ buf, int nx, int ny, int tc, int Bs, int off,
-                          double2 *__restrict__ quad) {
+// quad block entry of reference entry tt: packed symmetric entries keep
+// their index, xz/yz entries rc*nz + tr move to rc*(nz+1) + tr.
+__global__ void k_extract(const double2 *__restrict__ buf, int nx, int ny, int tc, int Bs, int off, int t0, int nz,
+                          int asym, double2 *__restrict__ quad) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     long total = (long)(nx + 1) * (ny + 1) * tc;
     if (idx >= total) return;
     int t = (int)(idx % tc);
     long q = idx / tc;
     int a = (int)(q / (ny + 1)), b = (int)(q - (long)a * (ny + 1));
-    quad[q * Bs + off + t] = buf[((long)a * 2 * ny + b) * tc + t];
+    int tt = t0 + t;
+    int dst = asym ? (tt / nz) * (nz + 1) + tt % nz : tt;
+    quad[q * Bs + off + dst] = buf[((long)a * 2 * ny + b) * tc + t];
 }
 
 // ---------------------------------------------------------------- host plan
@@ -631,7 +635,7 @@ std::vector<int> background_indices(const GreenModel &m) {
 }
 
 void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &quad, GreenBuildStats *stats,
-                 long *launches) {
+                 long *launches, Timers *tm) {
     auto t_start = std::chrono::steady_clock::now();
     EGX_CHECK(m.nx > 0 && m.ny > 0 && m.nz > 0 && m.dx > 0 && m.dy > 0, EGX_ERR_INVALID, "bad model dimensions");
     const int L = (int)m.bg_thick.size();
@@ -737,6 +741,7 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
     GreenDims gd{m.nx, m.ny, m.nz};
     const int Bs = gd.Bs();
     quad.ensure((size_t)gd.Q() * Bs * sizeof(double2));
+    EGX_CUDA(cudaMemsetAsync(quad.p, 0, (size_t)gd.Q() * Bs * sizeof(double2), s));  // row padding stays zero
 
     DevBuf d_lam, d_lay, d_trans, d_U, d_I, d_rho, d_gidx, d_flags, d_neg, d_radii, d_IA, d_IB, d_rowptr, d_terms,
         d_buf;
@@ -767,18 +772,24 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
             const int nl = (int)lams[it].size();
             double *dl = dev_upload(d_lam, lams[it], s);
             d_lay.ensure((size_t)6 * L * nl * sizeof(double2));
+            int ev = tm ? tm->begin(EGX_K_GREEN_LAYERS, s) : -1;
             k_layers<<<(nl + 127) / 128, 128, 0, s>>>(dl, nl, la, d_lay.as<double2>());
+            if (tm) tm->end(ev, s);
             long nthreads = (long)ntrans * nl;
+            ev = tm ? tm->begin(EGX_K_GREEN_KERNELS, s) : -1;
             k_kernels<<<(unsigned)((nthreads + 127) / 128), 128, 0, s>>>(dl, nl, d_lay.as<double2>(), la, dtrans,
                                                                           ntrans, which, d_U.as<double2>(), nl_total,
                                                                           col0[it]);
+            if (tm) tm->end(ev, s);
             const int nrho = (int)items[it].size();
             double *drho = dev_upload(d_rho, items[it], s);
             int *dg = dev_upload(d_gidx, gidx[it], s);
             long nh_threads = (long)nu * ntrans * nrho;
+            ev = tm ? tm->begin(EGX_K_GREEN_HANKEL, s) : -1;
             k_hankel<<<(unsigned)((nh_threads + 127) / 128), 128, 0, s>>>(d_U.as<double2>(), nu, ntrans, nl_total,
                                                                            col0[it], nrho, drho, dg, dflags, dneg,
                                                                            d_I.as<double2>(), nrad);
+            if (tm) tm->end(ev, s);
             // the per-item uploads above reuse buffers: finish before the next item
             EGX_CUDA(cudaStreamSynchronize(s));
             if (launches) *launches += 3;
@@ -820,18 +831,23 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
                 const int tcc = std::min(tc, blk - t0);
                 EGX_CUDA(cudaMemsetAsync(d_buf.p, 0, (size_t)cells4 * tcc * sizeof(double2), s));
                 dim3 grid(m.nx * m.ny, (tcc + 127) / 128);
+                int ev = tm ? tm->begin(EGX_K_GREEN_CELLS, s) : -1;
                 k_cells<<<grid, 128, 0, s>>>(drow, dterm, d_IA.as<double2>(), d_IB.as<double2>(), ntrans, nseg, m.nx,
                                              m.ny, t0, tcc, px[c], py[c], d_buf.as<double2>());
+                if (tm) tm->end(ev, s);
                 EGX_CUDA(cudaGetLastError());
+                ev = tm ? tm->begin(EGX_K_GREEN_FFT, s) : -1;
                 // y along all 2nx rows; x along ky <= ny, kx <= nx kept
                 const int n0 = 2 * m.nx, n1 = 2 * m.ny;
                 fft_lines<double>(d_buf.as<double2>(), n0, (long)n1 * tcc, tcc, tcc, n1, n1, p1, tw1.as<double2>(), -1,
                                   s, launches);
                 fft_lines<double>(d_buf.as<double2>(), m.ny + 1, tcc, (long)n1 * tcc, tcc, n0, m.nx + 1, p0,
                                   tw0.as<double2>(), -1, s, launches);
+                if (tm) tm->end(ev, s);
                 long n = (long)(m.nx + 1) * (m.ny + 1) * tcc;
                 k_extract<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_buf.as<double2>(), m.nx, m.ny, tcc, Bs,
-                                                                      offs[c] + t0, quad.as<double2>());
+                                                                      offs[c], t0, m.nz, c >= 4 ? 1 : 0,
+                                                                      quad.as<double2>());
                 EGX_CUDA(cudaGetLastError());
                 if (launches) *launches += 2;
             }

@@ -30,7 +30,7 @@ struct GreenBuildStats {
 // Build the spectral tensor into `quad` (device, complex128, layout of
 // GreenDims: quadrant points x [xx|xy|yy|zz|xz|yz] blocks).
 void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &quad, GreenBuildStats *stats,
-                 long *launches);
+                 long *launches, Timers *timers = nullptr);
 
 // Index of the background layer holding each anomaly layer; throws
 // EGX_ERR_MODEL when a layer straddles an interface (ModelUtils.cs:160-185).

@@ -335,9 +335,14 @@ double Gmres<T>::arnoldi(double bn, int &jh) {
         double dloo = 0, dnormw = 0;
         do {
             northo++;
+            const int koff = sizeof(T) == sizeof(double) ? 0 : EGX_K_C64;
+            int ev = timers ? timers->begin(EGX_K_GS_DOTS + koff, s_) : -1;
             VecOps<T>::multi_dot(V_, jh + 1, w_, n_, dots_, partials_, nblocks_, s_);
+            if (timers) timers->end(ev, s_);
+            ev = timers ? timers->begin(EGX_K_GS_UPDATE + koff, s_) : -1;
             VecOps<T>::update_norm(V_, jh + 1, dots_, w_, n_, norm_dev_, reinterpret_cast<double *>(partials_),
                                    nblocks_, s_);
+            if (timers) timers->end(ev, s_);
             kernel_launches += 4;
             EGX_CUDA(cudaMemcpyAsync(host_, dots_, sizeof(double2) * 64 + sizeof(double), cudaMemcpyDeviceToHost, s_));
             EGX_CUDA(cudaStreamSynchronize(s_));

@@ -60,10 +60,13 @@ class Gmres {
     // Solve(rightHandSide, initialGuess, result); result may alias
     // initialGuess; rhs may alias initialGuess (the inner preconditioner).
     GmresResult solve(const C<T> *rhs, const C<T> *x0, C<T> *result);
+    // the tolerance of the next solve (the workspace does not depend on it)
+    void set_tol(double tol) { tol_ = tol; }
     Fn apply;
     Fn precond;
     std::function<void(int, double)> on_iteration;
     long kernel_launches = 0;
+    Timers *timers = nullptr;
 
   private:
     double norm(const C<T> *x);

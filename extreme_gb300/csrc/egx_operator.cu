@@ -12,6 +12,9 @@
 //   k_lines     : inverse DFT along x, writing only the nx rows that are extracted;
 //   k_bwd_y     : inverse DFT along y, extraction with the backward factors and the
 //                 last step (ExtractData + PerformLastStep, :187-231).
+#include <algorithm>
+#include <type_traits>
+
 #include "egx_operator.cuh"
 
 namespace egx {
@@ -123,7 +126,7 @@ template <typename T, bool G_IN_SMEM>
 __global__ void k_contract(C<T> *buf, const C<T> *__restrict__ G, const OpDims d) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nz = d.nz;
-    const int S = nz * (nz + 1) / 2, A = nz * nz, Bs = 4 * S + 2 * A;
+    const int S = nz * (nz + 1) / 2, lda = nz + 1, A = nz * lda, Bs = 4 * S + 2 * A;
     const int q = blockIdx.x;
     const int a = q / (d.ny + 1), bq = q - a * (d.ny + 1);
     const int n1 = 2 * d.ny;
@@ -167,7 +170,7 @@ __global__ void k_contract(C<T> *buf, const C<T> *__restrict__ G, const OpDims d
                 int s = sym_index(i, j);
                 cfma<T>(a1, gxx[s], X[j]);
                 cfma<T>(a2, gxy[s], X[nz + j]);
-                cfma<T>(a3, gxz[i * nz + j], X[2 * nz + j]);
+                cfma<T>(a3, gxz[i * lda + j], X[2 * nz + j]);
             }
             // Sxy odd/odd, Axz odd in x
             if (mx != my) a2 = mk<T>(-a2.x, -a2.y);
@@ -177,14 +180,14 @@ __global__ void k_contract(C<T> *buf, const C<T> *__restrict__ G, const OpDims d
                 int s = sym_index(i, j);
                 cfma<T>(a1, gxy[s], X[j]);
                 cfma<T>(a2, gyy[s], X[nz + j]);
-                cfma<T>(a3, gyz[i * nz + j], X[2 * nz + j]);
+                cfma<T>(a3, gyz[i * lda + j], X[2 * nz + j]);
             }
             if (mx != my) a1 = mk<T>(-a1.x, -a1.y);
             if (my) a3 = mk<T>(-a3.x, -a3.y);
         } else {
             for (int j = 0; j < nz; j++) {
-                cfma<T>(a1, gxz[j * nz + i], X[j]);
-                cfma<T>(a2, gyz[j * nz + i], X[nz + j]);
+                cfma<T>(a1, gxz[j * lda + i], X[j]);
+                cfma<T>(a2, gyz[j * lda + i], X[nz + j]);
                 cfma<T>(a3, gzz[sym_index(i, j)], X[2 * nz + j]);
             }
             // -Axz^T x - Ayz^T y
@@ -207,15 +210,19 @@ static void set_smem(const void *fn, size_t bytes) {
 template <typename T>
 void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, const C<T> *x, C<T> *y, C<T> *buf,
                     const C<T> *tw0, const C<T> *tw1, const FftPlan &p0, const FftPlan &p1, cudaStream_t s,
-                    long *launches) {
+                    long *launches, Timers *tm, int *err) {
     const int n0 = 2 * d.nx, n1 = 2 * d.ny;
+    const int koff = sizeof(T) == sizeof(double) ? 0 : EGX_K_C64;
+    int ev;
     // 1. r*x, forward factors, zero padding, DFT along y (rows i < nx)
     {
         int bt = fft_cols(n1, sizeof(C<T>));
         size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
         set_smem<T>((const void *)k_fwd_y<T>, sm);
         dim3 grid(d.nx, (d.B + bt - 1) / bt);
+        ev = tm ? tm->begin(EGX_K_FWD_Y + koff, s) : -1;
         k_fwd_y<T><<<grid, threads_for(n1 * bt / 2), sm, s>>>(x, op, buf, d, p1, tw1, bt);
+        if (tm) tm->end(ev, s);
     }
     // 2. DFT along x over all columns; rows >= nx are zero
     {
@@ -223,8 +230,10 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
         size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
         set_smem<T>((const void *)k_lines<T>, sm);
         dim3 grid(n1, (d.B + bt - 1) / bt);
+        ev = tm ? tm->begin(EGX_K_FWD_X + koff, s) : -1;
         k_lines<T><<<grid, threads_for(n0 * bt / 2), sm, s>>>(buf, d.B, (long)n1 * d.B, d.B, d.nx, n0, p0, tw0, bt,
                                                               -1);
+        if (tm) tm->end(ev, s);
     }
     // 3. block contraction
     {
@@ -232,21 +241,29 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
         size_t sx = (size_t)4 * d.nrhs * 3 * d.nz * sizeof(C<T>);
         size_t sg = (size_t)gd.Bs() * sizeof(C<T>);
         int thr = 256;
-        if (sx + sg <= 200 * 1024) {
+        ev = tm ? tm->begin(EGX_K_CONTRACT + koff, s) : -1;
+        if (std::is_same<T, float>::value && err && contract_mma_fits(d.nz, d.nrhs)) {
+            launch_contract_mma(reinterpret_cast<float2 *>(buf), reinterpret_cast<const float2 *>(G), d, err, s);
+        } else if (std::is_same<T, float>::value && err && contract_c64_fits(d.nz, d.nrhs)) {
+            launch_contract_c64(reinterpret_cast<float2 *>(buf), reinterpret_cast<const float2 *>(G), d, err, s);
+        } else if (sx + sg <= 200 * 1024) {
             set_smem<T>((const void *)k_contract<T, true>, sx + sg);
             k_contract<T, true><<<(unsigned)gd.Q(), thr, sx + sg, s>>>(buf, G, d);
         } else {
             set_smem<T>((const void *)k_contract<T, false>, sx);
             k_contract<T, false><<<(unsigned)gd.Q(), thr, sx, s>>>(buf, G, d);
         }
+        if (tm) tm->end(ev, s);
     }
     // 4. inverse DFT along x; only rows < nx are needed afterwards
     {
         int bt = fft_cols(n0, sizeof(C<T>));
         size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
         dim3 grid(n1, (d.B + bt - 1) / bt);
+        ev = tm ? tm->begin(EGX_K_BWD_X + koff, s) : -1;
         k_lines<T><<<grid, threads_for(n0 * bt / 2), sm, s>>>(buf, d.B, (long)n1 * d.B, d.B, n0, d.nx, p0, tw0, bt,
                                                               +1);
+        if (tm) tm->end(ev, s);
     }
     // 5. inverse DFT along y, extraction, last step
     {
@@ -254,7 +271,9 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
         size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
         set_smem<T>((const void *)k_bwd_y<T>, sm);
         dim3 grid(d.nx, (d.B + bt - 1) / bt);
+        ev = tm ? tm->begin(EGX_K_BWD_Y + koff, s) : -1;
         k_bwd_y<T><<<grid, threads_for(n1 * bt / 2), sm, s>>>(buf, x, op, y, d, p1, tw1, bt);
+        if (tm) tm->end(ev, s);
     }
     EGX_CUDA(cudaGetLastError());
     if (launches) *launches += 5;
@@ -316,10 +335,11 @@ std::vector<double> twiddles(int n) {
 
 template void operator_apply<double>(const OpDims &, const OperatorData<double> &, const C<double> *,
                                      const C<double> *, C<double> *, C<double> *, const C<double> *,
-                                     const C<double> *, const FftPlan &, const FftPlan &, cudaStream_t, long *);
+                                     const C<double> *, const FftPlan &, const FftPlan &, cudaStream_t, long *,
+                                     Timers *, int *);
 template void operator_apply<float>(const OpDims &, const OperatorData<float> &, const C<float> *, const C<float> *,
                                     C<float> *, C<float> *, const C<float> *, const C<float> *, const FftPlan &,
-                                    const FftPlan &, cudaStream_t, long *);
+                                    const FftPlan &, cudaStream_t, long *, Timers *, int *);
 template void fft2d<double>(C<double> *, int, int, int, int, const C<double> *, const C<double> *, const FftPlan &,
                             const FftPlan &, cudaStream_t, long *);
 template void fft2d<float>(C<float> *, int, int, int, int, const C<float> *, const C<float> *, const FftPlan &,

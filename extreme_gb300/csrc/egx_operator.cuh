@@ -12,11 +12,14 @@ namespace egx {
 // xx, yy, zz even/even, xy odd/odd, xz odd in x, yz odd in y.
 // Per point, one contiguous block of Bs entries:
 //   xx | xy | yy | zz  (packed rc + tr*(tr+1)/2, S = nz(nz+1)/2 each)
-//   xz | yz            (rc*nz + tr, A = nz*nz each)
+//   xz | yz            (rc*(nz+1) + tr, A = nz*(nz+1) each: rows padded by one
+//                       entry so that reading a row or a column with one lane
+//                       per index is free of shared-memory bank conflicts)
 struct GreenDims {
     int nx, ny, nz;
     int S() const { return nz * (nz + 1) / 2; }
-    int A() const { return nz * nz; }
+    int lda() const { return nz + 1; }
+    int A() const { return nz * (nz + 1); }
     int Bs() const { return 4 * S() + 2 * A(); }
     long Q() const { return (long)(nx + 1) * (ny + 1); }
 };
@@ -39,7 +42,17 @@ struct OperatorData {
 template <typename T>
 void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, const C<T> *x, C<T> *y, C<T> *buf,
                     const C<T> *tw0, const C<T> *tw1, const FftPlan &p0, const FftPlan &p1, cudaStream_t s,
-                    long *launches);
+                    long *launches, Timers *timers = nullptr, int *err = nullptr);
+
+// complex64 contraction with TMA-staged blocks (egx_contract.cu); `err`
+// receives EGX_ERR_TIMEOUT if a bounded wait expires.
+bool contract_c64_fits(int nz, int nrhs);
+size_t contract_c64_smem(int nz, int nrhs);
+void launch_contract_c64(float2 *buf, const float2 *G, const OpDims &d, int *err, cudaStream_t s);
+// complex64 contraction on the tensor cores (egx_contract_mma.cu)
+bool contract_mma_fits(int nz, int nrhs);
+size_t contract_mma_smem(int nz, int nrhs);
+void launch_contract_mma(float2 *buf, const float2 *G, const OpDims &d, int *err, cudaStream_t s);
 
 // DFTs of `nlines` interleaved sequences: element e of line L, column b at
 // L*lstride + e*estride + b (b < B); elements e >= nload read as zero and

@@ -24,8 +24,18 @@ EXPORTS = [
     "egx_create", "egx_destroy", "egx_last_error", "egx_version", "egx_set_stream", "egx_launch_count",
     "egx_green_build", "egx_green_upload", "egx_green_download", "egx_green_free",
     "egx_op_prepare", "egx_op_apply", "egx_op_apply_c64", "egx_fft2d",
-    "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond",
+    "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products",
+    "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_read",
 ]
+
+# kernel kinds of egx_profile_read
+K_FWD_Y, K_FWD_X, K_CONTRACT, K_BWD_X, K_BWD_Y, K_GS_DOTS, K_GS_UPDATE = range(7)
+K_C64 = 8
+K_GREEN_LAYERS, K_GREEN_KERNELS, K_GREEN_HANKEL, K_GREEN_CELLS, K_GREEN_FFT = range(16, 21)
+KERNEL_NAMES = {K_FWD_Y: "fwd_y", K_FWD_X: "fwd_x", K_CONTRACT: "contract", K_BWD_X: "bwd_x", K_BWD_Y: "bwd_y",
+                K_GS_DOTS: "gs_dots", K_GS_UPDATE: "gs_update", K_GREEN_LAYERS: "green_layers",
+                K_GREEN_KERNELS: "green_kernels", K_GREEN_HANKEL: "green_hankel", K_GREEN_CELLS: "green_cells",
+                K_GREEN_FFT: "green_fft"}
 
 
 class EgxError(RuntimeError):
@@ -49,6 +59,10 @@ class GmresParams(C.Structure):
 class MixedParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_outer", C.c_int), ("m_out", C.c_int), ("m_in", C.c_int),
                 ("inner_tol", C.c_double), ("inner_restarts", C.c_int)]
+
+
+class SourceParams(C.Structure):
+    _fields_ = [("precision", C.c_int), ("fgmres", GmresParams), ("mixed", MixedParams)]
 
 
 class Result(C.Structure):
@@ -91,6 +105,13 @@ def load(path=None):
     lib.egx_fgmres_solve.argtypes = [vp, vp, vp, C.POINTER(GmresParams), C.POINTER(Result), i]
     lib.egx_mixed_solve.argtypes = [vp, vp, vp, C.POINTER(MixedParams), C.POINTER(Result), i]
     lib.egx_set_precond.argtypes = [vp, i, PRECOND_FN, vp]
+    lib.egx_dot_products.argtypes = [vp, vp, i, vp, C.c_long, vp, i]
+    lib.egx_normal_field.argtypes = [C.POINTER(Model), d, vp]
+    lib.egx_plane_wave.argtypes = [C.POINTER(Model), d, d, vp, vp]
+    lib.egx_solve_sources.argtypes = [vp, vp, vp, vp, vp, vp, vp, i, C.POINTER(SourceParams), vp, vp,
+                                      C.POINTER(Result), i]
+    lib.egx_profile.argtypes = [vp, i]
+    lib.egx_profile_read.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_double)]
     _lib = lib
     return lib
 
@@ -230,6 +251,62 @@ class Context:
             self._check(rc)
         return r.as_dict()
 
+    def dot_products(self, V, w):
+        """DotProductRequest: conj(V[:, k]) . w for every column of V [n, ncols]."""
+        Vt = np.ascontiguousarray(np.asarray(V, np.complex128).T)
+        w = _c128(w)
+        out = np.empty(Vt.shape[0], np.complex128)
+        self._check(self.lib.egx_dot_products(self.h, _ptr(Vt), Vt.shape[0], _ptr(w), w.size, _ptr(out), HOST))
+        return out
+
+    def solve_sources(self, green, zeta, zeta0, dz, e0, pols, precision=PREC_FP64, fgmres=None, mixed=None,
+                      want_chi=False, where=HOST, dev_ptrs=None):
+        """SolveForOneSource up to jQ for each (e0[i], pols[i]).
+
+        Host mode: zeta [nx,ny,nz], zeta0 [nz], e0 [nsrc, nz] complex128 arrays;
+        returns (jq [nsrc, N], chi or None, [result dicts]).
+        Device mode: dev_ptrs = dict(zeta=, zeta0=, e0=, jq=, chi=) device pointers."""
+        nsrc = len(pols)
+        pol = np.ascontiguousarray(pols, np.int32)
+        dz = np.ascontiguousarray(dz, np.float64)
+        fg = fgmres or {}
+        mx = mixed or {}
+        p = SourceParams(precision,
+                         GmresParams(fg.get("m_out", 15), fg.get("m_in", 10), fg.get("tol", 1e-8),
+                                     fg.get("max_restarts", 100), fg.get("precond", PRECOND_GMRES),
+                                     int(fg.get("check_true", True))),
+                         MixedParams(mx.get("tol", 1e-6), mx.get("max_outer", 10), mx.get("m_out", 30),
+                                     mx.get("m_in", 10), mx.get("inner_tol", 1e-4), mx.get("inner_restarts", 20)))
+        res = (Result * nsrc)()
+        if where == DEVICE:
+            d = dev_ptrs
+            rc = self.lib.egx_solve_sources(self.h, green.h, C.c_void_p(d["zeta"]), C.c_void_p(d["zeta0"]), _ptr(dz),
+                                            C.c_void_p(d["e0"]), _ptr(pol), nsrc, C.byref(p),
+                                            C.c_void_p(d.get("chi") or 0), C.c_void_p(d["jq"]), res, DEVICE)
+            if rc not in (OK, ERR_NOT_CONVERGED):
+                self._check(rc)
+            return [r.as_dict() for r in res]
+        z = _c128(zeta)
+        z0 = _c128(zeta0)
+        e = _c128(e0).reshape(nsrc, -1)
+        n = z.size * 3
+        jq = np.empty((nsrc, n), np.complex128)
+        chi = np.empty((nsrc, n), np.complex128) if want_chi else None
+        rc = self.lib.egx_solve_sources(self.h, green.h, _ptr(z), _ptr(z0), _ptr(dz), _ptr(e), _ptr(pol), nsrc,
+                                        C.byref(p), _ptr(chi) if want_chi else None, _ptr(jq), res, HOST)
+        if rc not in (OK, ERR_NOT_CONVERGED):
+            self._check(rc)
+        return jq, chi, [r.as_dict() for r in res]
+
+    def profile(self, enable=True):
+        self._check(self.lib.egx_profile(self.h, int(enable)))
+
+    def profile_read(self, kind):
+        n = C.c_long()
+        ms = C.c_double()
+        self._check(self.lib.egx_profile_read(self.h, kind, C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
     def set_precond(self, kind, fn=None):
         """fn(src_ptr, dst_ptr, n, precision) -> None, device pointers."""
         if kind == PRECOND_CALLBACK:
@@ -272,6 +349,29 @@ class GreenTensor:
             self.free()
         except Exception:
             pass
+
+
+def normal_field(model, omega):
+    """Thickness-averaged plane-wave E0 on each anomaly layer ([nz] complex)."""
+    lib = load()
+    m = model_struct(model)
+    out = np.empty(model.nz, np.complex128)
+    rc = lib.egx_normal_field(C.byref(m.s), float(omega), _ptr(out))
+    if rc != OK:
+        raise EgxError(rc, "normal field")
+    return out
+
+
+def plane_wave(model, omega, depth):
+    """(E, H) of the 1-D plane wave at a flat depth."""
+    lib = load()
+    m = model_struct(model)
+    e = np.empty(1, np.complex128)
+    h = np.empty(1, np.complex128)
+    rc = lib.egx_plane_wave(C.byref(m.s), float(omega), float(depth), _ptr(e), _ptr(h))
+    if rc != OK:
+        raise EgxError(rc, "plane wave")
+    return complex(e[0]), complex(h[0])
 
 
 class _ModelStruct:

@@ -1,0 +1,90 @@
+"""Host-side mirror of the reference's forward-solver surface for the IE hot
+path, backed by ``libegx.so``.
+
+* :class:`ForwardSettings` -- ``Extreme.Cartesian/Forward/Project/ForwardSettings.cs:8-12``
+  (same names and class defaults);
+* :class:`Mt3DForwardSolver` -- ``Extreme.Cartesian.Magnetotellurics/Solver/Mt3DForwardSolver.cs:78-129``:
+  ``solve(model, frequency)`` computes the anomaly-to-anomaly Green tensor
+  (``CalculateGreenTensor``) and then solves polarisation X and Y
+  (``SolveForOneSource``: normal field, ``jS``, ``chi0``, FGMRES, ``Es``, ``jQ``).
+
+Everything numeric runs in the CUDA library: the host only forms the
+per-layer plane-wave field (``egx_normal_field``, ``nz`` scalars) and the
+complex conductivities ``zeta = sigma - i omega eps0``.
+"""
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import egx
+from .model import EPS0, CartesianModel, freq_to_omega
+
+
+@dataclass
+class ForwardSettings:
+    residual: float = 1e-8
+    inner_buffer_length: int = 10
+    outer_buffer_length: int = 15
+    max_repeats_number: int = 100
+    number_of_hankels: int = 10
+
+
+@dataclass
+class MixedSettings:
+    """Precision form: inner complex64 FGMRES inside FP64 refinement."""
+    tol: float = 1e-6
+    max_outer: int = 10
+    m_out: int = 30
+    m_in: int = 10
+    inner_tol: float = 1e-4
+    inner_restarts: int = 20
+
+
+@dataclass
+class MtSolution:
+    frequency: float
+    jq: np.ndarray                      # [2, N]: pol X, pol Y
+    chi: Optional[np.ndarray]
+    results: List[dict] = field(default_factory=list)
+
+
+def model_zeta(model: CartesianModel, omega: float):
+    """Anomaly and background complex conductivities (OmegaModelUtils.cs:57-83)."""
+    zeta = model.sigma.astype(np.complex128) - 1j * omega * EPS0
+    bg = model.background_indices()
+    zb = model.section.sigma.astype(np.complex128) - 1j * omega * EPS0
+    return np.ascontiguousarray(zeta), np.ascontiguousarray(zb[bg])
+
+
+class Mt3DForwardSolver:
+    def __init__(self, settings: ForwardSettings = None, precision=egx.PREC_FP64, mixed: MixedSettings = None,
+                 ctx: egx.Context = None, device=0):
+        self.settings = settings or ForwardSettings()
+        self.precision = precision
+        self.mixed = mixed or MixedSettings()
+        self.ctx = ctx or egx.Context(device)
+
+    def calculate_green_tensor(self, model: CartesianModel, frequency: float):
+        omega = freq_to_omega(frequency)
+        return self.ctx.green_build(model, omega, self.settings.number_of_hankels, self.precision)
+
+    def solve(self, model: CartesianModel, frequency: float, green=None, want_chi=False) -> MtSolution:
+        omega = freq_to_omega(frequency)
+        own = green is None
+        if own:
+            green = self.calculate_green_tensor(model, frequency)
+        try:
+            zeta, zeta0 = model_zeta(model, omega)
+            e0 = egx.normal_field(model, omega)
+            s = self.settings
+            fg = dict(m_out=s.outer_buffer_length, m_in=s.inner_buffer_length, tol=s.residual,
+                      max_restarts=s.max_repeats_number)
+            mx = self.mixed.__dict__
+            jq, chi, res = self.ctx.solve_sources(green, zeta, zeta0, model.layer_thickness,
+                                                  np.stack([e0, e0]), [0, 1], precision=self.precision,
+                                                  fgmres=fg, mixed=mx, want_chi=want_chi)
+        finally:
+            if own:
+                green.free()
+        return MtSolution(frequency, jq, chi, res)

@@ -82,7 +82,9 @@ typedef struct {
     double tol;           /* target relative true residual of the outer loop */
     int max_outer;        /* refinement steps */
     int m_out, m_in;      /* inner FGMRES buffers */
-    double inner_tol;     /* relative tolerance of each inner solve */
+    double inner_tol;     /* tightest relative tolerance asked of an inner solve;
+                             a refinement at true residual be asks only for
+                             max(inner_tol, min(0.5, 0.3 * tol / be)) */
     int inner_restarts;
 } egx_mixed_params;
 
@@ -154,6 +156,48 @@ int egx_mixed_solve(egx_ctx *ctx, const double *b, double *x, const egx_mixed_pa
 /* RightPreconditionerRequest plug point: kind EGX_PRECOND_CALLBACK routes
  * z_j = M(v_j) of the outer FGMRES to fn(user, ...). */
 int egx_set_precond(egx_ctx *ctx, int kind, egx_precond_fn fn, void *user);
+
+/* DotProductRequest (AnomalyCurrentFgmresSolver.cs:115-130): out[k] =
+ * conj(V[:, k])^T w for k < ncols, V column-major with leading dimension n. */
+int egx_dot_products(egx_ctx *ctx, const double *V, int ncols, const double *w, long n, double *out, int where);
+
+/* ---- MT source and the CIE pipeline around the solve ------------------- */
+/* Thickness-averaged 1-D plane-wave field on each anomaly layer
+ * (Mt3DForwardSolver.CalculateNormalFieldFromSource, Mt3DForwardSolver.cs:251-275;
+ * PlaneWaveCalculator.CalculateFieldE, PlaneWaveCalculator.cs:11-40). e0: [nz] complex. */
+int egx_normal_field(const egx_model *model, double omega, double *e0);
+/* Plane-wave E and H at a flat depth (PlaneWaveCalculator.CalculateFieldE/H,
+ * PlaneWaveCalculator.cs:11-64). e, h: one complex each. */
+int egx_plane_wave(const egx_model *model, double omega, double depth, double *e, double *h);
+
+typedef struct {
+    int precision;              /* EGX_PREC_FP64: complex128 FGMRES; EGX_PREC_MIXED: mixed solve */
+    egx_gmres_params fgmres;    /* used with EGX_PREC_FP64 */
+    egx_mixed_params mixed;     /* used with EGX_PREC_MIXED */
+} egx_source_params;
+
+/* ForwardSolverGenerics.SolveForOneSource up to jQ for nsrc sources
+ * (Forward/ForwardSolverGenerics.cs:30-50, Forward/ForwardSolver.cs:186-436):
+ * jS = (zeta - zeta0) E0, chi0 = K_chi0 jS, solve A chi = chi0 from x0 = chi0,
+ * Es = (2 sqrt(Re zeta0) chi - jS)/(zeta + conj zeta0), jQ = Es (zeta - zeta0) + jS.
+ * e0: [nsrc][nz] complex normal field per layer, pol: [nsrc] component
+ * (0 = x, 1 = y); chi (may be NULL), jq: [nsrc][N]; res: [nsrc]. */
+int egx_solve_sources(egx_ctx *ctx, egx_green *g, const double *zeta, const double *zeta0, const double *dz,
+                      const double *e0, const int *pol, int nsrc, const egx_source_params *p, double *chi,
+                      double *jq, egx_result *res, int where);
+
+/* ---- per-kernel device time ---------------------------------------------- */
+/* Instrumented kernels; add EGX_K_C64 for the complex64 variants. */
+enum {
+    EGX_K_FWD_Y = 0, EGX_K_FWD_X = 1, EGX_K_CONTRACT = 2, EGX_K_BWD_X = 3, EGX_K_BWD_Y = 4,
+    EGX_K_GS_DOTS = 5, EGX_K_GS_UPDATE = 6, EGX_K_C64 = 8,
+    EGX_K_GREEN_LAYERS = 16, EGX_K_GREEN_KERNELS = 17, EGX_K_GREEN_HANKEL = 18, EGX_K_GREEN_CELLS = 19,
+    EGX_K_GREEN_FFT = 20
+};
+/* enable != 0 records CUDA events around every instrumented launch. */
+int egx_profile(egx_ctx *ctx, int enable);
+/* Launches and summed device milliseconds of one kernel kind since enable. */
+int egx_profile_read(egx_ctx *ctx, int kind, long *launches, double *total_ms);
 
 #ifdef __cplusplus
 }

@@ -79,6 +79,26 @@ def test_contraction_matches_reference_c(gold):
     assert rel(mine, gold["ref_full_zgemv"]) < 1e-14
 
 
+def test_threaded_c_contraction_matches_golden(gold):
+    """The C restatement timed as the CPU baseline gives the reference's
+    FullZgemv golden output too, and agrees with the numpy oracle on a
+    ragged random case."""
+    from oracle import ccontract
+    m, _ = _tiny()
+    P = 4 * m.nx * m.ny
+    G = {c: gold["oracle_G_" + c].reshape(P, -1) for c in ("xx", "xy", "yy", "zz", "xz", "yz")}
+    src = gold["contract_src"].reshape(P, 3, m.nz)
+    assert rel(ccontract.contract(G, src, m.nz, 2).reshape(-1), gold["ref_full_zgemv"]) < 1e-14
+    rng = np.random.default_rng(5)
+    nz, pts = 13, (3, 7)
+    s = nz * (nz + 1) // 2
+    G = {c: rng.standard_normal(pts + (s,)) + 1j * rng.standard_normal(pts + (s,)) for c in ("xx", "xy", "yy", "zz")}
+    for c in ("xz", "yz"):
+        G[c] = rng.standard_normal(pts + (nz * nz,)) + 1j * rng.standard_normal(pts + (nz * nz,))
+    x = rng.standard_normal(pts + (3, nz)) + 1j * rng.standard_normal(pts + (3, nz))
+    assert rel(ccontract.contract(G, x, nz), op.contract(G, x, nz)) < 1e-14
+
+
 @pytest.mark.skipif(ref.load() is None, reason="oracle/_ref not built (needs the reference tree)")
 def test_exp_sums_live_reference_small_model():
     """Live comparison on the 32x32x8 model when the reference C is built here."""
