@@ -470,10 +470,8 @@ int egx_green_build(egx_ctx *ctx, const egx_model *model, double omega, int n_ha
         build_green(gm, n_hankels, ctx->stream, g->g64, &st, &ctx->launches, &ctx->timers);
         if (precision == EGX_PREC_MIXED) {
             GreenDims gd{gm.nx, gm.ny, gm.nz};
-            long n = gd.Q() * gd.Bs();
-            g->g32.ensure(n * sizeof(float2));
-            convert_d2f(g->g64.as<double2>(), g->g32.as<float2>(), n, 1.0, ctx->stream);
-            ctx->launches++;
+            g->g32.ensure(green_c64_entries(gd) * sizeof(float2));
+            green_to_c64(g->g64.as<double2>(), g->g32.as<float2>(), gd, ctx->stream, &ctx->launches);
             g->has32 = true;
         }
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -498,9 +496,9 @@ int egx_green_upload(egx_ctx *ctx, int nx, int ny, int nz, const double *const c
         g->g64.ensure(q.size() * sizeof(cd));
         EGX_CUDA(cudaMemcpyAsync(g->g64.p, q.data(), q.size() * sizeof(cd), cudaMemcpyHostToDevice, ctx->stream));
         if (precision == EGX_PREC_MIXED) {
-            g->g32.ensure(q.size() * sizeof(float2));
-            convert_d2f(g->g64.as<double2>(), g->g32.as<float2>(), (long)q.size(), 1.0, ctx->stream);
-            ctx->launches++;
+            GreenDims gd{nx, ny, nz};
+            g->g32.ensure(green_c64_entries(gd) * sizeof(float2));
+            green_to_c64(g->g64.as<double2>(), g->g32.as<float2>(), gd, ctx->stream, &ctx->launches);
             g->has32 = true;
         }
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -1,0 +1,480 @@
+// Block contraction of the CIE operator in complex64 on the tensor cores
+// (ConvolutionOperator.ApplyGreenTensorAlongZ, ConvolutionOperator.cs:274-327)
+// for nz in {16, 32, 48}, one or two right-hand sides per pass, reading the
+// complex64 Green copy in a 4x4 sub-block layout.
+//
+// Sub-block layout of one stored spectral point (nb = nz/4):
+//   xx | xy | yy | zz : the nb(nb+1)/2 upper-triangle 4x4 sub-blocks (I <= J)
+//                       of the symmetric block, sub-block I + J(J+1)/2,
+//                       element (i%4)*4 + (j%4); diagonal sub-blocks whole;
+//   xz | yz           : all nb*nb sub-blocks, sub-block I*nb + J, element
+//                       (rc%4)*4 + (tr%4).
+// Every fragment load of a half-warp (4 rows x 4 columns of G, either
+// orientation) then falls in one 128-byte sub-block: conflict-free.
+//
+// Algebra as in the other contraction kernels: the four spectral points
+// sharing a stored block are right-hand sides of one (3nz x 3nz) complex
+// matrix after D_p sign flips, the complex product is embedded in real
+// arithmetic [Yr | Yi] = Gr [Xr | Xi] + Gi [-Xi | Xr], and each TF32 operand
+// is split into a rounded high part and a remainder (three products per
+// pair: hi.hi + hi.lo + lo.hi), which keeps complex64 accuracy.
+//
+// Work split per CTA (one per SM, loop over stored points): 9 warps as
+// 3 row groups x 3 column groups; each warp owns 1/3 of the 16-row tiles and
+// 1/3 of the 8-column tiles, keeps the offsets of its A fragments in
+// registers (built once), and accumulates one partial product per row tile.
+// The -A^T blocks (z rows, x|y columns) are exactly the tiles of row group 2
+// and column groups 0 and 1, so their sign goes onto those warps' B
+// fragments. Column groups 1 and 2 leave partials in shared memory; group 0
+// adds them and stores.
+//
+// Per stored point: one TMA bulk copy of the block and one per present
+// right-hand-side segment into one of two stages, issued two points ahead
+// and completing on the stage's mbarrier (waits bounded to 2 s; on expiry
+// EGX_ERR_TIMEOUT is recorded in *err and the kernel returns).
+#include <algorithm>
+#include <cstdint>
+
+#include "egx_krylov.cuh"
+#include "egx_operator.cuh"
+
+namespace egx {
+
+namespace {
+
+__device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t gtime_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ bool bar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
+    const uint64_t t0 = gtime_ns();
+    while (!bar_try(bar, parity))
+        if (gtime_ns() - t0 > limit_ns) return false;
+    return true;
+}
+
+__device__ __forceinline__ void bar_expect(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ float2 lds64(uint32_t a) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+    return v;
+}
+
+__device__ __forceinline__ uint4 lds128(uint32_t a) {
+    uint4 v;
+    asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a));
+    return v;
+}
+
+__device__ __forceinline__ void sts128(uint32_t a, uint4 v) {
+    asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+                 : "memory");
+}
+
+// TF32 high part rounded to nearest (ties away from zero) on the magnitude
+__device__ __forceinline__ uint32_t tf32_hi(uint32_t bits) { return (bits + 0x1000u) & 0xffffe000u; }
+
+// a = hi + lo, hi TF32; the tensor core reads the top 19 bits of lo
+__device__ __forceinline__ void split(float a, uint32_t &hi, uint32_t &lo) {
+    hi = tf32_hi(__float_as_uint(a));
+    lo = __float_as_uint(a - __uint_as_float(hi));
+}
+
+// both parts rounded (right-hand sides: split once per point)
+__device__ __forceinline__ void split_rn(float a, uint32_t &hi, uint32_t &lo) {
+    hi = tf32_hi(__float_as_uint(a));
+    lo = tf32_hi(__float_as_uint(a - __uint_as_float(hi)));
+}
+
+__device__ __forceinline__ void mma_tf32(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+constexpr uint64_t kWait = 2000000000ull;
+
+__host__ __device__ inline int sb_sym(int nz) { return (nz / 4) * (nz / 4 + 1) / 2 * 16; }
+__host__ __device__ inline int sb_asy(int nz) { return (nz / 4) * (nz / 4) * 16; }
+
+// index in the sub-block layout of the entry G(row, col) of the 3nz x 3nz
+// point operator, up to the sign of the -A^T blocks
+__host__ __device__ inline int sb_index(int nz, int row, int col) {
+    const int co = row / nz, i = row - co * nz, ci = col / nz, j = col - ci * nz;
+    const int S = sb_sym(nz), A = sb_asy(nz), nb = nz / 4;
+    if ((co < 2 && ci < 2) || (co == 2 && ci == 2)) {
+        const int c = (co == 2) ? 3 : ((co == 0 && ci == 0) ? 0 : ((co == 1 && ci == 1) ? 2 : 1));
+        int I = i >> 2, J = j >> 2, a = i & 3, b = j & 3;
+        if (I > J) {
+            int s = I;
+            I = J;
+            J = s;
+            s = a;
+            a = b;
+            b = s;
+        }
+        return c * S + (I + J * (J + 1) / 2) * 16 + a * 4 + b;
+    }
+    if (ci == 2) return 4 * S + co * A + ((i >> 2) * nb + (j >> 2)) * 16 + (i & 3) * 4 + (j & 3);
+    return 4 * S + ci * A + ((j >> 2) * nb + (i >> 2)) * 16 + (j & 3) * 4 + (i & 3);
+}
+
+// complex128 packed quadrant (GreenDims layout) -> complex64 sub-block layout
+__global__ void k_repack_sb(const double2 *__restrict__ g64, float2 *__restrict__ g32, long Q, int nz) {
+    const int S = sb_sym(nz), A = sb_asy(nz), BS = 4 * S + 2 * A, nb = nz / 4;
+    // packed layout (GreenDims): S0 per symmetric block, rows of xz/yz padded to nz + 1
+    const int S0 = nz * (nz + 1) / 2, lda = nz + 1, A0 = nz * lda, BS0 = 4 * S0 + 2 * A0;
+    const long total = Q * BS;
+    for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+        const long q = idx / BS;
+        const int d = (int)(idx - q * BS);
+        int src;
+        if (d < 4 * S) {
+            const int c = d / S, r = d - c * S, sbi = r >> 4, e = r & 15;
+            int J = 0;
+            while ((J + 1) * (J + 2) / 2 <= sbi) J++;
+            const int I = sbi - J * (J + 1) / 2;
+            const int i = 4 * I + (e >> 2), j = 4 * J + (e & 3);
+            const int lo = i < j ? i : j, hi = i < j ? j : i;
+            src = c * S0 + lo + hi * (hi + 1) / 2;
+        } else {
+            const int d2 = d - 4 * S, co = d2 / A, r = d2 - co * A, sbi = r >> 4, e = r & 15;
+            const int I = sbi / nb, J = sbi - I * nb;
+            src = 4 * S0 + co * A0 + (4 * I + (e >> 2)) * lda + 4 * J + (e & 3);
+        }
+        const double2 v = g64[q * BS0 + src];
+        g32[idx] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
+template <int NZ, int NRHS>
+struct Sb {
+    static constexpr int R = 3 * NZ, MT = R / 16, KT = R / 8, NB = NZ / 4;
+    static constexpr int SYM = NB * (NB + 1) / 2 * 16, ASY = NB * NB * 16, BS = 4 * SYM + 2 * ASY;
+    static constexpr int MG = 3, KG = 3, MPW = MT / MG, KPW = KT / KG;
+    static constexpr int THREADS = 32 * MG * KG;
+    static constexpr int XB = NRHS * R;  // complex per spectral point and pass
+    static constexpr uint32_t G_BYTES = BS * 8u;
+    static constexpr uint32_t X_BYTES = 4u * XB * 8u;
+    static constexpr uint32_t BF_BYTES = KT * NRHS * 2u * 32u * 16u;
+    static constexpr uint32_t PART_BYTES = (KG - 1) * MT * 4u * NRHS * 32u * 4u;
+    static constexpr uint32_t OFF_X = 2 * G_BYTES, OFF_BF = OFF_X + 2 * X_BYTES, OFF_PART = OFF_BF + BF_BYTES;
+    static constexpr uint32_t SMEM = OFF_PART + PART_BYTES;
+    static_assert(MT % MG == 0 && KT % KG == 0, "tile counts must split over the warp grid");
+    static_assert(G_BYTES % 128 == 0 && X_BYTES % 128 == 0, "stage alignment");
+};
+
+template <int NZ, int NRHS>
+__global__ void __launch_bounds__(Sb<NZ, NRHS>::THREADS, 1)
+    k_contract_sb(float2 *buf, const float2 *__restrict__ G, const int nx, const int ny, const int B, const int rhs0,
+                  int *err) {
+    using P = Sb<NZ, NRHS>;
+    constexpr int R = P::R, MPW = P::MPW, KPW = P::KPW;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int status;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int mg = warp % P::MG, kg = warp / P::MG;
+    const uint32_t sG = saddr(smem), sX = sG + P::OFF_X, sBF = sG + P::OFF_BF, sPART = sG + P::OFF_PART;
+    const uint32_t bar0 = saddr(&bars[0]);
+    const long Q = (long)(nx + 1) * (ny + 1);
+    const int n1 = 2 * ny;
+
+    // offsets (complex units) of this lane's A-fragment entries: pair
+    // (row tile mg*MPW + im, column tile kg*KPW + ik), entries e = 0..3, two
+    // 16-bit offsets per word; computed through the (still unused) stage-0
+    // block buffer and then held in registers
+    constexpr int TABN = MPW * KPW * 2;
+    static_assert(P::MG * P::KG * TABN * 32 * 4 <= P::G_BYTES, "offset scratch must fit in one stage");
+    uint32_t tab[TABN];
+    {
+        uint32_t *scratch = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * TABN * 32 + lane;
+#pragma unroll 1
+        for (int p = 0; p < MPW * KPW; p++) {
+            const int im = p / KPW, ik = p - im * KPW;
+            const int r0 = 16 * (mg * MPW + im) + g, c0 = 8 * (kg * KPW + ik) + t;
+            scratch[(2 * p) * 32] = (uint32_t)sb_index(NZ, r0, c0) | ((uint32_t)sb_index(NZ, r0 + 8, c0) << 16);
+            scratch[(2 * p + 1) * 32] =
+                (uint32_t)sb_index(NZ, r0, c0 + 4) | ((uint32_t)sb_index(NZ, r0 + 8, c0 + 4) << 16);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < TABN; j++) tab[j] = scratch[j * 32];
+    }
+    // the -A^T tiles: z rows (row group 2) x x|y columns (column groups 0, 1)
+    const uint32_t bsign = (mg == 2 && kg < 2) ? 0x80000000u : 0u;
+
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        status = 0;
+    }
+    __syncthreads();
+
+    auto issue = [&](long qq, int stage) {
+        const int a = (int)(qq / (ny + 1)), bq = (int)(qq - (long)a * (ny + 1));
+        const int nkx = (a == 0 || a == nx) ? 1 : 2;
+        const int nky = (bq == 0 || bq == ny) ? 1 : 2;
+        const uint32_t bar = bar0 + 8 * stage;
+        bar_expect(bar, P::G_BYTES + (uint32_t)(nkx * nky) * (P::XB * 8u));
+        bulk_g2s(sG + stage * P::G_BYTES, G + qq * P::BS, P::G_BYTES, bar);
+        for (int p = 0; p < 4; p++) {
+            const int mx = p >> 1, my = p & 1;
+            if (mx < nkx && my < nky) {
+                const long pt = (long)(mx ? 2 * nx - a : a) * n1 + (my ? 2 * ny - bq : bq);
+                bulk_g2s(sX + stage * P::X_BYTES + p * (P::XB * 8u), buf + pt * B + (long)rhs0 * R, P::XB * 8u, bar);
+            }
+        }
+    };
+    long q = blockIdx.x;
+    if (tid == 0) {
+        if (q < Q) issue(q, 0);
+        if (q + gridDim.x < Q) issue(q + gridDim.x, 1);
+    }
+
+    for (int it = 0; q < Q; q += gridDim.x, it++) {
+        const int stage = it & 1;
+        const uint32_t parity = (it >> 1) & 1;
+        const uint32_t bar = bar0 + 8 * stage;
+        if (tid == 0 && !bar_wait(bar, parity, kWait)) status = 1;
+        __syncthreads();
+        if (status) {
+            if (tid == 0) {
+                atomicExch(err, EGX_ERR_TIMEOUT);
+                bar_wait(bar0 + 8 * (stage ^ 1), ((it + 1) >> 1) & 1, kWait);
+            }
+            return;
+        }
+        bar_wait(bar, parity, kWait);  // acquire the stage for every thread
+        const int a = (int)(q / (ny + 1)), bq = (int)(q - (long)a * (ny + 1));
+        const int nkx = (a == 0 || a == nx) ? 1 : 2;
+        const int nky = (bq == 0 || bq == ny) ? 1 : 2;
+
+        // B fragments, split once: entry (kt, rhs, part, lane), part 0 = [Xr | Xi], 1 = [-Xi | Xr]
+        const uint32_t sXq = sX + stage * P::X_BYTES;
+        for (int e = tid; e < P::KT * NRHS * 32; e += P::THREADS) {
+            const int ln = e & 31, rest = e >> 5, r = rest % NRHS, kt = rest / NRHS;
+            const int gg = ln >> 2, tt = ln & 3;
+            const int v = gg & 3, mx = v >> 1, my = v & 1;
+            const bool im = gg >= 4, present = mx < nkx && my < nky;
+            uint32_t w[8];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int k = 8 * kt + tt + 4 * h;
+                float2 x = make_float2(0.f, 0.f);
+                if (present) {
+                    x = lds64(sXq + (uint32_t)(v * P::XB + r * R + k) * 8u);
+                    const int comp = k / NZ;
+                    if ((comp == 0 && mx) || (comp == 1 && my)) x = make_float2(-x.x, -x.y);
+                }
+                split_rn(im ? x.y : x.x, w[h], w[2 + h]);
+                split_rn(im ? x.x : -x.y, w[4 + h], w[6 + h]);
+            }
+            const uint32_t base = sBF + (uint32_t)((kt * NRHS + r) * 2) * 512u + ln * 16u;
+            sts128(base, make_uint4(w[0], w[1], w[2], w[3]));
+            sts128(base + 512u, make_uint4(w[4], w[5], w[6], w[7]));
+        }
+        __syncthreads();
+
+        float acc[MPW][NRHS][4];
+#pragma unroll
+        for (int im = 0; im < MPW; im++)
+#pragma unroll
+            for (int r = 0; r < NRHS; r++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[im][r][c] = 0.f;
+        const uint32_t sGq = sG + stage * P::G_BYTES;
+#pragma unroll
+        for (int ik = 0; ik < KPW; ik++) {
+            const int kt = kg * KPW + ik;
+            uint4 b1[NRHS], b2[NRHS];
+#pragma unroll
+            for (int r = 0; r < NRHS; r++) {
+                const uint32_t base = sBF + (uint32_t)((kt * NRHS + r) * 2) * 512u + lane * 16u;
+                b1[r] = lds128(base);
+                b2[r] = lds128(base + 512u);
+                b1[r].x ^= bsign;
+                b1[r].y ^= bsign;
+                b1[r].z ^= bsign;
+                b1[r].w ^= bsign;
+                b2[r].x ^= bsign;
+                b2[r].y ^= bsign;
+                b2[r].z ^= bsign;
+                b2[r].w ^= bsign;
+            }
+#pragma unroll
+            for (int im = 0; im < MPW; im++) {
+                const uint32_t t0 = tab[(im * KPW + ik) * 2], t1 = tab[(im * KPW + ik) * 2 + 1];
+                const uint32_t off[4] = {t0 & 0xffffu, t0 >> 16, t1 & 0xffffu, t1 >> 16};
+                uint32_t arh[4], arl[4], aih[4], ail[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const float2 gv = lds64(sGq + off[e] * 8u);
+                    split(gv.x, arh[e], arl[e]);
+                    split(gv.y, aih[e], ail[e]);
+                }
+#pragma unroll
+                for (int r = 0; r < NRHS; r++) {
+                    mma_tf32(acc[im][r], arh, b1[r].x, b1[r].y);
+                    mma_tf32(acc[im][r], aih, b2[r].x, b2[r].y);
+                    mma_tf32(acc[im][r], arh, b1[r].z, b1[r].w);
+                    mma_tf32(acc[im][r], aih, b2[r].z, b2[r].w);
+                    mma_tf32(acc[im][r], arl, b1[r].x, b1[r].y);
+                    mma_tf32(acc[im][r], ail, b2[r].x, b2[r].y);
+                }
+            }
+        }
+        __syncthreads();  // the stage and the B fragments are free
+        if (tid == 0 && q + 2L * gridDim.x < Q) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(q + 2L * gridDim.x, stage);
+        }
+        // column groups 1, 2 -> shared partials [kg-1][mt][r][c][lane]
+        if (kg > 0) {
+#pragma unroll
+            for (int im = 0; im < MPW; im++)
+#pragma unroll
+                for (int r = 0; r < NRHS; r++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const int mt = mg * MPW + im;
+                        const uint32_t o = (uint32_t)((((kg - 1) * P::MT + mt) * NRHS + r) * 4 + c) * 128u + lane * 4u;
+                        asm volatile("st.shared.f32 [%0], %1;" ::"r"(sPART + o), "f"(acc[im][r][c]) : "memory");
+                    }
+        }
+        __syncthreads();
+        if (kg == 0) {
+#pragma unroll
+            for (int im = 0; im < MPW; im++) {
+                const int mt = mg * MPW + im;
+#pragma unroll
+                for (int r = 0; r < NRHS; r++) {
+                    float y[4];
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        float s = acc[im][r][c];
+#pragma unroll
+                        for (int k = 0; k < P::KG - 1; k++) {
+                            const uint32_t o = (uint32_t)(((k * P::MT + mt) * NRHS + r) * 4 + c) * 128u + lane * 4u;
+                            float p;
+                            asm volatile("ld.shared.f32 %0, [%1];" : "=f"(p) : "r"(sPART + o));
+                            s += p;
+                        }
+                        y[c] = s;
+                    }
+                    // C: rows g, g+8; columns 2t, 2t+1 (t < 2: Re of v = 2t, 2t+1; t >= 2: Im of v = 2t-4, 2t-3)
+                    float o[4];
+#pragma unroll
+                    for (int c = 0; c < 4; c++) o[c] = __shfl_xor_sync(0xffffffffu, y[c], 2);
+                    if (t < 2) {
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const int row = 16 * mt + g + 8 * (c >> 1);
+                            const int v = 2 * t + (c & 1);
+                            const int mx = v >> 1, my = v & 1;
+                            if (mx < nkx && my < nky) {
+                                float2 val = make_float2(y[c], o[c]);
+                                const int comp = row / NZ;
+                                if ((comp == 0 && mx) || (comp == 1 && my)) val = make_float2(-val.x, -val.y);
+                                const long pt = (long)(mx ? 2 * nx - a : a) * n1 + (my ? 2 * ny - bq : bq);
+                                buf[pt * B + (long)(rhs0 + r) * R + row] = val;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int NZ, int NRHS>
+void launch_sb(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err, cudaStream_t s, int nsm) {
+    using P = Sb<NZ, NRHS>;
+    static bool attr = false;
+    if (!attr) {
+        EGX_CUDA(cudaFuncSetAttribute((const void *)k_contract_sb<NZ, NRHS>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM));
+        attr = true;
+    }
+    const long Q = (long)(d.nx + 1) * (d.ny + 1);
+    const unsigned grid = (unsigned)std::min<long>(Q, nsm);
+    k_contract_sb<NZ, NRHS><<<grid, P::THREADS, P::SMEM, s>>>(buf, G, d.nx, d.ny, d.B, rhs0, err);
+    EGX_CUDA(cudaGetLastError());
+}
+
+template <int NZ>
+void launch_nz(float2 *buf, const float2 *G, const OpDims &d, int *err, cudaStream_t s, int nsm, long *launches) {
+    for (int r0 = 0; r0 < d.nrhs;) {
+        if (d.nrhs - r0 >= 2) {
+            launch_sb<NZ, 2>(buf, G, d, r0, err, s, nsm);
+            r0 += 2;
+        } else {
+            launch_sb<NZ, 1>(buf, G, d, r0, err, s, nsm);
+            r0 += 1;
+        }
+        if (launches) ++*launches;
+    }
+}
+
+}  // namespace
+
+bool sb_layout(int nz) { return nz == 16 || nz == 32 || nz == 48; }
+
+long sb_block(int nz) { return 4L * sb_sym(nz) + 2L * sb_asy(nz); }
+
+long green_c64_entries(const GreenDims &gd) { return gd.Q() * (sb_layout(gd.nz) ? sb_block(gd.nz) : (long)gd.Bs()); }
+
+void green_to_c64(const double2 *g64, float2 *g32, const GreenDims &gd, cudaStream_t s, long *launches) {
+    if (sb_layout(gd.nz)) {
+        const long total = gd.Q() * sb_block(gd.nz);
+        const unsigned blocks = (unsigned)std::min<long>((total + 255) / 256, 152L * 64);
+        k_repack_sb<<<blocks, 256, 0, s>>>(g64, g32, gd.Q(), gd.nz);
+        EGX_CUDA(cudaGetLastError());
+    } else {
+        convert_d2f(g64, g32, gd.Q() * gd.Bs(), 1.0, s);
+    }
+    if (launches) ++*launches;
+}
+
+void launch_contract_sb(float2 *buf, const float2 *G, const OpDims &d, int *err, cudaStream_t s, long *launches) {
+    static int nsm = 0;
+    if (!nsm) EGX_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, 0));
+    switch (d.nz) {
+        case 16: launch_nz<16>(buf, G, d, err, s, nsm, launches); break;
+        case 32: launch_nz<32>(buf, G, d, err, s, nsm, launches); break;
+        case 48: launch_nz<48>(buf, G, d, err, s, nsm, launches); break;
+        default: throw Error(EGX_ERR_INVALID, "sub-block contraction needs nz in {16, 32, 48}");
+    }
+}
+
+}  // namespace egx

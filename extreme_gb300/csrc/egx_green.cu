@@ -613,14 +613,18 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 
 }  // namespace
 
+// ModelUtils.FindCorrespondingBackgroundLayerIndex (ModelUtils.cs:27-50)
+// sums depths and thicknesses in C# decimal; integer micrometres keep those
+// sums exact here for every length given to 1e-6 m.
 std::vector<int> background_indices(const GreenModel &m) {
+    auto um = [](double v) { return std::llround(v * 1e6); };
     std::vector<int> out(m.nz);
     for (int k = 0; k < m.nz; k++) {
-        double start = m.depth[k], end = m.depth[k] + m.thick[k];
-        double ss = m.zero_air_level;
+        const long long start = um(m.depth[k]), end = um(m.depth[k]) + um(m.thick[k]);
+        long long ss = um(m.zero_air_level);
         int found = -1;
         for (size_t i = 0; i < m.bg_thick.size(); i++) {
-            double es = ss + m.bg_thick[i];
+            const long long es = ss + um(m.bg_thick[i]);
             if (start >= ss && end <= es) {
                 found = (int)i;
                 break;

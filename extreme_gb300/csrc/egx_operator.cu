@@ -242,7 +242,14 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
         size_t sg = (size_t)gd.Bs() * sizeof(C<T>);
         int thr = 256;
         ev = tm ? tm->begin(EGX_K_CONTRACT + koff, s) : -1;
-        if (std::is_same<T, float>::value && err && contract_mma_fits(d.nz, d.nrhs)) {
+        if (std::is_same<T, float>::value && sb_layout(d.nz)) {
+            // the complex64 copy is in the sub-block layout for these nz
+            EGX_CHECK(err, EGX_ERR_INVALID, "complex64 contraction needs the device error flag");
+            long extra = 0;
+            launch_contract_sb(reinterpret_cast<float2 *>(buf), reinterpret_cast<const float2 *>(G), d, err, s,
+                               &extra);
+            if (launches) *launches += extra - 1;
+        } else if (std::is_same<T, float>::value && err && contract_mma_fits(d.nz, d.nrhs)) {
             launch_contract_mma(reinterpret_cast<float2 *>(buf), reinterpret_cast<const float2 *>(G), d, err, s);
         } else if (std::is_same<T, float>::value && err && contract_c64_fits(d.nz, d.nrhs)) {
             launch_contract_c64(reinterpret_cast<float2 *>(buf), reinterpret_cast<const float2 *>(G), d, err, s);

@@ -49,6 +49,14 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
 bool contract_c64_fits(int nz, int nrhs);
 size_t contract_c64_smem(int nz, int nrhs);
 void launch_contract_c64(float2 *buf, const float2 *G, const OpDims &d, int *err, cudaStream_t s);
+// complex64 Green copy and contraction in the 4x4 sub-block layout
+// (egx_contract_sb.cu), used for every complex64 apply when sb_layout(nz);
+// other nz keep the packed layout of GreenDims.
+bool sb_layout(int nz);
+long sb_block(int nz);                      // complex entries per stored point
+long green_c64_entries(const GreenDims &gd);  // size of the complex64 copy
+void green_to_c64(const double2 *g64, float2 *g32, const GreenDims &gd, cudaStream_t s, long *launches);
+void launch_contract_sb(float2 *buf, const float2 *G, const OpDims &d, int *err, cudaStream_t s, long *launches);
 // complex64 contraction on the tensor cores (egx_contract_mma.cu)
 bool contract_mma_fits(int nz, int nrhs);
 size_t contract_mma_smem(int nz, int nrhs);

@@ -78,12 +78,16 @@ class CartesianModel:
 
     def background_index(self, k):
         """Background layer that contains anomaly layer ``k``
-        (``ModelUtils.FindCorrespondingBackgroundLayerIndex``)."""
-        start = self.layer_depth[k]
-        end = start + self.layer_thickness[k]
-        ss = self.section.zero_air_level
+        (``ModelUtils.FindCorrespondingBackgroundLayerIndex``,
+        ``Extreme.Cartesian/Model/ModelUtils.cs:27-50``). The reference sums in
+        C# decimal; integer micrometres keep the sums exact here."""
+        def um(v):
+            return int(round(float(v) * 1e6))
+        start = um(self.layer_depth[k])
+        end = start + um(self.layer_thickness[k])
+        ss = um(self.section.zero_air_level)
         for i in range(self.section.n_layers):
-            es = ss + self.section.thickness[i]
+            es = ss + um(self.section.thickness[i])
             if start >= ss and end <= es:
                 return i
             ss = es

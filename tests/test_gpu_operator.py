@@ -90,6 +90,29 @@ def test_apply_small_matches_oracle(egx_ctx, small_case, op_type):
     g.free()
 
 
+@pytest.mark.parametrize("nz", [16, 32, 48])
+def test_c64_subblock_apply_matches_oracle(egx_ctx, nz):
+    """complex64 apply on the sub-block Green layout (nz in {16, 32, 48}),
+    one to three right-hand sides (passes of two and one), ragged edges
+    (nx != ny, the kx = 0, nx and ky = 0, ny points with fewer mirrors)."""
+    from extreme_gb300.model import freq_to_omega, scaled_model
+    m = scaled_model(10, 6, nz, seed=3)
+    f = m.frequencies[2]
+    om = OmegaModel.build(m, f)
+    g = egx_ctx.green_build(m, freq_to_omega(f), 10, egx.PREC_MIXED)
+    G = g.download()
+    egx_ctx.op_prepare(g, om.zeta, om.zeta0, m.layer_thickness, op.OP_A)
+    rng = np.random.default_rng(nz)
+    n = m.nx * m.ny * 3 * m.nz
+    xs = rng.standard_normal((3, n)) + 1j * rng.standard_normal((3, n))
+    want = [op.apply(G, om, xs[i], op.OP_A) for i in range(3)]
+    for nrhs in (1, 2, 3):
+        y = egx_ctx.op_apply_c64(xs[:nrhs].reshape(-1).astype(np.complex64), nrhs=nrhs)
+        for i in range(nrhs):
+            assert rel(y[i * n:(i + 1) * n], want[i]) < 2e-5, (nrhs, i)
+    g.free()
+
+
 def test_apply_before_prepare_is_state_error():
     ctx = egx.Context(0)
     with pytest.raises(egx.EgxError) as e:
