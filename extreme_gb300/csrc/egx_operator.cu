@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <type_traits>
 
+#include "egx_fft_reg.cuh"
 #include "egx_operator.cuh"
 
 namespace egx {
@@ -120,6 +121,121 @@ __global__ void k_bwd_y(const C<T> *__restrict__ buf, const C<T> *__restrict__ x
     }
 }
 
+// ------------------------------------------------------------------
+// The same three steps on the register-resident DFT (egx_fft_reg.cuh) for
+// lengths in {64, 128, 256, 512}: one CTA per line and 128-byte tile of
+// columns, every global access a whole 128-byte row segment.
+template <typename T, int N>
+__global__ void __launch_bounds__(reg_threads<N, T>())
+    k_fwd_y_r(const C<T> *__restrict__ x, const OperatorData<T> op, C<T> *__restrict__ buf, const OpDims d,
+              const C<T> *__restrict__ tw) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int BT = RegCols<T>::BT;
+    const int i = blockIdx.x;
+    const int b = blockIdx.y * BT + (int)(threadIdx.x % BT);
+    const bool bok = b < d.B;
+    const int per = 3 * d.nz;
+    const int rhs = bok ? b / per : 0, rem = b - rhs * per, k = rem % d.nz;
+    const C<T> f = bok ? op.fwd[k] : mk<T>(0, 0);
+    const C<T> *xr = x + rhs * d.nvec + rem;
+    auto load = [&](int j) -> C<T> {
+        if (!bok || j >= d.ny) return mk<T>(0, 0);
+        const long cell = (long)i * d.ny + j;
+        return cmul<T>(f, cmul<T>(op.r[cell * d.nz + k], xr[cell * per]));
+    };
+    auto store = [&](int j, C<T> v) {
+        if (bok) buf[((long)i * N + j) * d.B + b] = v;
+    };
+    fft_reg<T, N>(reinterpret_cast<C<T> *>(smem_raw), tw, -1, load, store);
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(reg_threads<N, T>())
+    k_lines_r(C<T> *buf, long lstride, long estride, int B, int nload, int nstore, const C<T> *__restrict__ tw,
+              int sign) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int BT = RegCols<T>::BT;
+    const int b = blockIdx.y * BT + (int)(threadIdx.x % BT);
+    const bool bok = b < B;
+    C<T> *line = buf + (long)blockIdx.x * lstride + b;
+    auto load = [&](int e) -> C<T> { return (bok && e < nload) ? line[e * estride] : mk<T>(0, 0); };
+    auto store = [&](int e, C<T> v) {
+        if (bok && e < nstore) line[e * estride] = v;
+    };
+    fft_reg<T, N>(reinterpret_cast<C<T> *>(smem_raw), tw, sign, load, store);
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(reg_threads<N, T>())
+    k_bwd_y_r(const C<T> *__restrict__ buf, const C<T> *__restrict__ x, const OperatorData<T> op,
+              C<T> *__restrict__ y, const OpDims d, const C<T> *__restrict__ tw) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int BT = RegCols<T>::BT;
+    const int i = blockIdx.x;
+    const int b = blockIdx.y * BT + (int)(threadIdx.x % BT);
+    const bool bok = b < d.B;
+    const int per = 3 * d.nz;
+    const int rhs = bok ? b / per : 0, rem = b - rhs * per, k = rem % d.nz;
+    const C<T> bw = bok ? op.bwd[k] : mk<T>(0, 0);
+    const C<T> *row = buf + (long)i * N * d.B + b;
+    auto load = [&](int j) -> C<T> { return bok ? row[(long)j * d.B] : mk<T>(0, 0); };
+    auto store = [&](int j, C<T> v) {
+        if (!bok || j >= d.ny) return;
+        const long cell = (long)i * d.ny + j;
+        const long idx = rhs * d.nvec + cell * per + rem;
+        const C<T> yv = cmul<T>(bw, v);
+        const C<T> xv = x[idx];
+        const C<T> rx = cmul<T>(op.r[cell * d.nz + k], xv);
+        y[idx] = (op.type == EGX_OP_A) ? csub<T>(csub<T>(xv, yv), rx) : cadd<T>(yv, rx);
+    };
+    fft_reg<T, N>(reinterpret_cast<C<T> *>(smem_raw), tw, +1, load, store);
+}
+
+template <typename T, int N>
+static void reg_attr(const void *fn) {
+    constexpr size_t sm = reg_smem<N, T>();
+    if (sm > 48 * 1024) EGX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+}
+
+// which: 0 fwd_y, 1 lines, 2 bwd_y
+template <typename T, int N>
+static void launch_reg(int which, dim3 grid, cudaStream_t s, const C<T> *x, const OperatorData<T> *op, C<T> *buf,
+                       C<T> *y, const OpDims *d, long lstride, long estride, int B, int nload, int nstore,
+                       const C<T> *tw, int sign) {
+    constexpr size_t sm = reg_smem<N, T>();
+    constexpr int thr = reg_threads<N, T>();
+    if (which == 0) {
+        static bool a = false;
+        if (!a) reg_attr<T, N>((const void *)k_fwd_y_r<T, N>), a = true;
+        k_fwd_y_r<T, N><<<grid, thr, sm, s>>>(x, *op, buf, *d, tw);
+    } else if (which == 1) {
+        static bool a = false;
+        if (!a) reg_attr<T, N>((const void *)k_lines_r<T, N>), a = true;
+        k_lines_r<T, N><<<grid, thr, sm, s>>>(buf, lstride, estride, B, nload, nstore, tw, sign);
+    } else {
+        static bool a = false;
+        if (!a) reg_attr<T, N>((const void *)k_bwd_y_r<T, N>), a = true;
+        k_bwd_y_r<T, N><<<grid, thr, sm, s>>>(buf, x, *op, y, *d, tw);
+    }
+}
+
+// returns false when n has no register plan
+template <typename T>
+static bool run_reg(int n, int which, int nlines, int B, cudaStream_t s, const C<T> *x, const OperatorData<T> *op,
+                    C<T> *buf, C<T> *y, const OpDims *d, long lstride, long estride, int nload, int nstore,
+                    const C<T> *tw, int sign) {
+    if (!reg_fft_ok(n)) return false;
+    constexpr int BT = RegCols<T>::BT;
+    dim3 grid(nlines, (B + BT - 1) / BT);
+    switch (n) {
+        case 64: launch_reg<T, 64>(which, grid, s, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
+        case 128: launch_reg<T, 128>(which, grid, s, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
+        case 256: launch_reg<T, 256>(which, grid, s, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
+        default: launch_reg<T, 512>(which, grid, s, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
+    }
+    return true;
+}
+
 // Block contraction, one CTA per stored quadrant point (a, b). The block is
 // staged in shared memory when it fits (G_IN_SMEM), else read through L1.
 template <typename T, bool G_IN_SMEM>
@@ -216,23 +332,28 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
     int ev;
     // 1. r*x, forward factors, zero padding, DFT along y (rows i < nx)
     {
-        int bt = fft_cols(n1, sizeof(C<T>));
-        size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
-        set_smem<T>((const void *)k_fwd_y<T>, sm);
-        dim3 grid(d.nx, (d.B + bt - 1) / bt);
         ev = tm ? tm->begin(EGX_K_FWD_Y + koff, s) : -1;
-        k_fwd_y<T><<<grid, threads_for(n1 * bt / 2), sm, s>>>(x, op, buf, d, p1, tw1, bt);
+        if (!run_reg<T>(n1, 0, d.nx, d.B, s, x, &op, buf, nullptr, &d, 0, 0, 0, 0, tw1, -1)) {
+            int bt = fft_cols(n1, sizeof(C<T>));
+            size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
+            set_smem<T>((const void *)k_fwd_y<T>, sm);
+            dim3 grid(d.nx, (d.B + bt - 1) / bt);
+            k_fwd_y<T><<<grid, threads_for(n1 * bt / 2), sm, s>>>(x, op, buf, d, p1, tw1, bt);
+        }
         if (tm) tm->end(ev, s);
     }
     // 2. DFT along x over all columns; rows >= nx are zero
     {
-        int bt = fft_cols(n0, sizeof(C<T>));
-        size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
-        set_smem<T>((const void *)k_lines<T>, sm);
-        dim3 grid(n1, (d.B + bt - 1) / bt);
         ev = tm ? tm->begin(EGX_K_FWD_X + koff, s) : -1;
-        k_lines<T><<<grid, threads_for(n0 * bt / 2), sm, s>>>(buf, d.B, (long)n1 * d.B, d.B, d.nx, n0, p0, tw0, bt,
-                                                              -1);
+        if (!run_reg<T>(n0, 1, n1, d.B, s, nullptr, nullptr, buf, nullptr, nullptr, d.B, (long)n1 * d.B, d.nx, n0,
+                        tw0, -1)) {
+            int bt = fft_cols(n0, sizeof(C<T>));
+            size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
+            set_smem<T>((const void *)k_lines<T>, sm);
+            dim3 grid(n1, (d.B + bt - 1) / bt);
+            k_lines<T><<<grid, threads_for(n0 * bt / 2), sm, s>>>(buf, d.B, (long)n1 * d.B, d.B, d.nx, n0, p0, tw0,
+                                                                  bt, -1);
+        }
         if (tm) tm->end(ev, s);
     }
     // 3. block contraction
@@ -264,22 +385,28 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
     }
     // 4. inverse DFT along x; only rows < nx are needed afterwards
     {
-        int bt = fft_cols(n0, sizeof(C<T>));
-        size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
-        dim3 grid(n1, (d.B + bt - 1) / bt);
         ev = tm ? tm->begin(EGX_K_BWD_X + koff, s) : -1;
-        k_lines<T><<<grid, threads_for(n0 * bt / 2), sm, s>>>(buf, d.B, (long)n1 * d.B, d.B, n0, d.nx, p0, tw0, bt,
-                                                              +1);
+        if (!run_reg<T>(n0, 1, n1, d.B, s, nullptr, nullptr, buf, nullptr, nullptr, d.B, (long)n1 * d.B, n0, d.nx,
+                        tw0, +1)) {
+            int bt = fft_cols(n0, sizeof(C<T>));
+            size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
+            set_smem<T>((const void *)k_lines<T>, sm);
+            dim3 grid(n1, (d.B + bt - 1) / bt);
+            k_lines<T><<<grid, threads_for(n0 * bt / 2), sm, s>>>(buf, d.B, (long)n1 * d.B, d.B, n0, d.nx, p0, tw0,
+                                                                  bt, +1);
+        }
         if (tm) tm->end(ev, s);
     }
     // 5. inverse DFT along y, extraction, last step
     {
-        int bt = fft_cols(n1, sizeof(C<T>));
-        size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
-        set_smem<T>((const void *)k_bwd_y<T>, sm);
-        dim3 grid(d.nx, (d.B + bt - 1) / bt);
         ev = tm ? tm->begin(EGX_K_BWD_Y + koff, s) : -1;
-        k_bwd_y<T><<<grid, threads_for(n1 * bt / 2), sm, s>>>(buf, x, op, y, d, p1, tw1, bt);
+        if (!run_reg<T>(n1, 2, d.nx, d.B, s, x, &op, buf, y, &d, 0, 0, 0, 0, tw1, +1)) {
+            int bt = fft_cols(n1, sizeof(C<T>));
+            size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
+            set_smem<T>((const void *)k_bwd_y<T>, sm);
+            dim3 grid(d.nx, (d.B + bt - 1) / bt);
+            k_bwd_y<T><<<grid, threads_for(n1 * bt / 2), sm, s>>>(buf, x, op, y, d, p1, tw1, bt);
+        }
         if (tm) tm->end(ev, s);
     }
     EGX_CUDA(cudaGetLastError());
@@ -289,7 +416,8 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
 template <typename T>
 void fft2d(C<T> *buf, int n0, int n1, int howmany, int sign, const C<T> *tw0, const C<T> *tw1, const FftPlan &p0,
            const FftPlan &p1, cudaStream_t s, long *launches) {
-    {
+    if (!run_reg<T>(n1, 1, n0, howmany, s, nullptr, nullptr, buf, nullptr, nullptr, (long)n1 * howmany, howmany, n1,
+                    n1, tw1, sign)) {
         int bt = fft_cols(n1, sizeof(C<T>));
         size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
         set_smem<T>((const void *)k_lines<T>, sm);
@@ -297,7 +425,8 @@ void fft2d(C<T> *buf, int n0, int n1, int howmany, int sign, const C<T> *tw0, co
         k_lines<T><<<grid, threads_for(n1 * bt / 2), sm, s>>>(buf, (long)n1 * howmany, howmany, howmany, n1, n1, p1,
                                                               tw1, bt, sign);
     }
-    {
+    if (!run_reg<T>(n0, 1, n1, howmany, s, nullptr, nullptr, buf, nullptr, nullptr, howmany, (long)n1 * howmany, n0,
+                    n0, tw0, sign)) {
         int bt = fft_cols(n0, sizeof(C<T>));
         size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
         set_smem<T>((const void *)k_lines<T>, sm);
@@ -312,6 +441,12 @@ void fft2d(C<T> *buf, int n0, int n1, int howmany, int sign, const C<T> *tw0, co
 template <typename T>
 void fft_lines(C<T> *buf, int nlines, long lstride, long estride, int B, int nload, int nstore, const FftPlan &p,
                const C<T> *tw, int sign, cudaStream_t s, long *launches) {
+    if (run_reg<T>(p.n, 1, nlines, B, s, nullptr, nullptr, buf, nullptr, nullptr, lstride, estride, nload, nstore, tw,
+                   sign)) {
+        EGX_CUDA(cudaGetLastError());
+        if (launches) *launches += 1;
+        return;
+    }
     int bt = fft_cols(p.n, sizeof(C<T>));
     size_t sm = 2 * (size_t)p.n * bt * sizeof(C<T>);
     set_smem<T>((const void *)k_lines<T>, sm);
