@@ -86,12 +86,6 @@ __device__ __forceinline__ float2 lds64(uint32_t a) {
     return v;
 }
 
-__device__ __forceinline__ uint4 lds128(uint32_t a) {
-    uint4 v;
-    asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a));
-    return v;
-}
-
 __device__ __forceinline__ void sts128(uint32_t a, uint4 v) {
     asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
                  : "memory");
@@ -113,7 +107,7 @@ __device__ __forceinline__ void split_rn(float a, uint32_t &hi, uint32_t &lo) {
 }
 
 __device__ __forceinline__ void mma_tf32(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
-    asm volatile(
+    asm(
         "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
         "{%0,%1,%2,%3};"
         : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
@@ -179,17 +173,26 @@ template <int NZ, int NRHS>
 struct Sb {
     static constexpr int R = 3 * NZ, MT = R / 16, KT = R / 8, NB = NZ / 4;
     static constexpr int SYM = NB * (NB + 1) / 2 * 16, ASY = NB * NB * 16, BS = 4 * SYM + 2 * ASY;
-    static constexpr int MG = 3, KG = 3, MPW = MT / MG, KPW = KT / KG;
+    // 3 row groups x 4 column groups: 12 warps, 3 per SM sub-partition;
+    // column group kg owns column tiles [kt0(kg), kt0(kg + 1))
+    static constexpr int MG = 3, KG = 4, MPW = MT / MG, KMAX = (KT + KG - 1) / KG;
     static constexpr int THREADS = 32 * MG * KG;
     static constexpr int XB = NRHS * R;  // complex per spectral point and pass
     static constexpr uint32_t G_BYTES = BS * 8u;
     static constexpr uint32_t X_BYTES = 4u * XB * 8u;
     static constexpr uint32_t BF_BYTES = KT * NRHS * 2u * 32u * 16u;
-    static constexpr uint32_t PART_BYTES = (KG - 1) * MT * 4u * NRHS * 32u * 4u;
-    static constexpr uint32_t OFF_X = 2 * G_BYTES, OFF_BF = OFF_X + 2 * X_BYTES, OFF_PART = OFF_BF + BF_BYTES;
-    static constexpr uint32_t SMEM = OFF_PART + PART_BYTES;
-    static_assert(MT % MG == 0 && KT % KG == 0, "tile counts must split over the warp grid");
+    static constexpr uint32_t PART_BYTES = KG * MT * 4u * NRHS * 32u * 4u;
+    // partial sums get their own region when it fits, else they reuse the
+    // B fragments (one more barrier per point)
+    static constexpr bool PART_ALIAS = 2 * G_BYTES + 2 * X_BYTES + BF_BYTES + PART_BYTES > 227u * 1024u;
+    static constexpr uint32_t OFF_X = 2 * G_BYTES, OFF_BF = OFF_X + 2 * X_BYTES;
+    static constexpr uint32_t OFF_PART = PART_ALIAS ? OFF_BF : OFF_BF + BF_BYTES;
+    static constexpr uint32_t SMEM = PART_ALIAS ? OFF_BF + BF_BYTES : OFF_PART + PART_BYTES;
+    static_assert(MT % MG == 0, "row tiles must split over the row groups");
+    static_assert(!PART_ALIAS || PART_BYTES <= BF_BYTES, "partials must fit in the B-fragment region");
+    static_assert(MT <= MG * KG, "one warp per row tile in the epilogue");
     static_assert(G_BYTES % 128 == 0 && X_BYTES % 128 == 0, "stage alignment");
+    __host__ __device__ static constexpr int kt0(int kg) { return kg * KT / KG; }
 };
 
 template <int NZ, int NRHS>
@@ -197,41 +200,44 @@ __global__ void __launch_bounds__(Sb<NZ, NRHS>::THREADS, 1)
     k_contract_sb(float2 *buf, const float2 *__restrict__ G, const int nx, const int ny, const int B, const int rhs0,
                   int *err) {
     using P = Sb<NZ, NRHS>;
-    constexpr int R = P::R, MPW = P::MPW, KPW = P::KPW;
+    constexpr int R = P::R, MPW = P::MPW, KMAX = P::KMAX;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int status;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t = lane & 3;
     const int mg = warp % P::MG, kg = warp / P::MG;
-    const uint32_t sG = saddr(smem), sX = sG + P::OFF_X, sBF = sG + P::OFF_BF, sPART = sG + P::OFF_PART;
+    const int ktb = P::kt0(kg), kcnt = P::kt0(kg + 1) - ktb;
+    const uint32_t sG = saddr(smem), sX = sG + P::OFF_X, sBF = sG + P::OFF_BF;
     const uint32_t bar0 = saddr(&bars[0]);
     const long Q = (long)(nx + 1) * (ny + 1);
     const int n1 = 2 * ny;
 
     // offsets (complex units) of this lane's A-fragment entries: pair
-    // (row tile mg*MPW + im, column tile kg*KPW + ik), entries e = 0..3, two
+    // (row tile mg*MPW + im, column tile ktb + ik), entries e = 0..3, two
     // 16-bit offsets per word; computed through the (still unused) stage-0
     // block buffer and then held in registers
-    constexpr int TABN = MPW * KPW * 2;
+    constexpr int TABN = MPW * KMAX * 2;
     static_assert(P::MG * P::KG * TABN * 32 * 4 <= P::G_BYTES, "offset scratch must fit in one stage");
     uint32_t tab[TABN];
     {
         uint32_t *scratch = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * TABN * 32 + lane;
 #pragma unroll 1
-        for (int p = 0; p < MPW * KPW; p++) {
-            const int im = p / KPW, ik = p - im * KPW;
-            const int r0 = 16 * (mg * MPW + im) + g, c0 = 8 * (kg * KPW + ik) + t;
-            scratch[(2 * p) * 32] = (uint32_t)sb_index(NZ, r0, c0) | ((uint32_t)sb_index(NZ, r0 + 8, c0) << 16);
-            scratch[(2 * p + 1) * 32] =
-                (uint32_t)sb_index(NZ, r0, c0 + 4) | ((uint32_t)sb_index(NZ, r0 + 8, c0 + 4) << 16);
+        for (int p = 0; p < MPW * KMAX; p++) {
+            const int im = p / KMAX, ik = p - im * KMAX;
+            uint32_t w0 = 0, w1 = 0;
+            if (ik < kcnt) {
+                const int r0 = 16 * (mg * MPW + im) + g, c0 = 8 * (ktb + ik) + t;
+                w0 = (uint32_t)sb_index(NZ, r0, c0) | ((uint32_t)sb_index(NZ, r0 + 8, c0) << 16);
+                w1 = (uint32_t)sb_index(NZ, r0, c0 + 4) | ((uint32_t)sb_index(NZ, r0 + 8, c0 + 4) << 16);
+            }
+            scratch[(2 * p) * 32] = w0;
+            scratch[(2 * p + 1) * 32] = w1;
         }
         __syncwarp();
 #pragma unroll
         for (int j = 0; j < TABN; j++) tab[j] = scratch[j * 32];
     }
-    // the -A^T tiles: z rows (row group 2) x x|y columns (column groups 0, 1)
-    const uint32_t bsign = (mg == 2 && kg < 2) ? 0x80000000u : 0u;
 
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
@@ -313,16 +319,22 @@ __global__ void __launch_bounds__(Sb<NZ, NRHS>::THREADS, 1)
             for (int r = 0; r < NRHS; r++)
 #pragma unroll
                 for (int c = 0; c < 4; c++) acc[im][r][c] = 0.f;
-        const uint32_t sGq = sG + stage * P::G_BYTES;
+        // plain shared-memory reads: the compiler may schedule them freely
+        // between the barriers that order them against the stage's TMA and
+        // the B-fragment pass
+        const float2 *Gq = reinterpret_cast<const float2 *>(smem + stage * P::G_BYTES);
+        const uint4 *BFq = reinterpret_cast<const uint4 *>(smem + P::OFF_BF) + lane;
 #pragma unroll
-        for (int ik = 0; ik < KPW; ik++) {
-            const int kt = kg * KPW + ik;
+        for (int ik = 0; ik < KMAX; ik++) {
+            if (ik >= kcnt) break;
+            const int kt = ktb + ik;
+            // the -A^T tiles: z rows (row group 2) x x|y columns
+            const uint32_t bsign = (mg == 2 && kt < 2 * NZ / 8) ? 0x80000000u : 0u;
             uint4 b1[NRHS], b2[NRHS];
 #pragma unroll
             for (int r = 0; r < NRHS; r++) {
-                const uint32_t base = sBF + (uint32_t)((kt * NRHS + r) * 2) * 512u + lane * 16u;
-                b1[r] = lds128(base);
-                b2[r] = lds128(base + 512u);
+                b1[r] = BFq[((kt * NRHS + r) * 2) * 32];
+                b2[r] = BFq[((kt * NRHS + r) * 2 + 1) * 32];
                 b1[r].x ^= bsign;
                 b1[r].y ^= bsign;
                 b1[r].z ^= bsign;
@@ -332,64 +344,65 @@ __global__ void __launch_bounds__(Sb<NZ, NRHS>::THREADS, 1)
                 b2[r].z ^= bsign;
                 b2[r].w ^= bsign;
             }
+            // A fragments of all row tiles of this column tile: [im][re hi, re lo, im hi, im lo][e]
+            uint32_t af[MPW][4][4];
 #pragma unroll
             for (int im = 0; im < MPW; im++) {
-                const uint32_t t0 = tab[(im * KPW + ik) * 2], t1 = tab[(im * KPW + ik) * 2 + 1];
+                const uint32_t t0 = tab[(im * KMAX + ik) * 2], t1 = tab[(im * KMAX + ik) * 2 + 1];
                 const uint32_t off[4] = {t0 & 0xffffu, t0 >> 16, t1 & 0xffffu, t1 >> 16};
-                uint32_t arh[4], arl[4], aih[4], ail[4];
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
-                    const float2 gv = lds64(sGq + off[e] * 8u);
-                    split(gv.x, arh[e], arl[e]);
-                    split(gv.y, aih[e], ail[e]);
-                }
-#pragma unroll
-                for (int r = 0; r < NRHS; r++) {
-                    mma_tf32(acc[im][r], arh, b1[r].x, b1[r].y);
-                    mma_tf32(acc[im][r], aih, b2[r].x, b2[r].y);
-                    mma_tf32(acc[im][r], arh, b1[r].z, b1[r].w);
-                    mma_tf32(acc[im][r], aih, b2[r].z, b2[r].w);
-                    mma_tf32(acc[im][r], arl, b1[r].x, b1[r].y);
-                    mma_tf32(acc[im][r], ail, b2[r].x, b2[r].y);
+                    const float2 gv = Gq[off[e]];
+                    split(gv.x, af[im][0][e], af[im][1][e]);
+                    split(gv.y, af[im][2][e], af[im][3][e]);
                 }
             }
+            // six products per right-hand side; consecutive MMAs go to
+            // different row tiles, so their accumulator chains overlap
+#pragma unroll
+            for (int r = 0; r < NRHS; r++) {
+#pragma unroll
+                for (int im = 0; im < MPW; im++) mma_tf32(acc[im][r], af[im][0], b1[r].x, b1[r].y);
+#pragma unroll
+                for (int im = 0; im < MPW; im++) mma_tf32(acc[im][r], af[im][2], b2[r].x, b2[r].y);
+#pragma unroll
+                for (int im = 0; im < MPW; im++) mma_tf32(acc[im][r], af[im][0], b1[r].z, b1[r].w);
+#pragma unroll
+                for (int im = 0; im < MPW; im++) mma_tf32(acc[im][r], af[im][2], b2[r].z, b2[r].w);
+#pragma unroll
+                for (int im = 0; im < MPW; im++) mma_tf32(acc[im][r], af[im][1], b1[r].x, b1[r].y);
+#pragma unroll
+                for (int im = 0; im < MPW; im++) mma_tf32(acc[im][r], af[im][3], b2[r].x, b2[r].y);
+            }
         }
-        __syncthreads();  // the stage and the B fragments are free
+        // partial sums [kg][mt][r][c][lane]; when they reuse the B-fragment
+        // region every warp must be done with its fragments first
+        float *PART = reinterpret_cast<float *>(smem + P::OFF_PART) + lane;
+        if (P::PART_ALIAS) __syncthreads();
+#pragma unroll
+        for (int im = 0; im < MPW; im++)
+#pragma unroll
+            for (int r = 0; r < NRHS; r++)
+#pragma unroll
+                for (int c = 0; c < 4; c++)
+                    PART[(((kg * P::MT + mg * MPW + im) * NRHS + r) * 4 + c) * 32] = acc[im][r][c];
+        __syncthreads();  // the stage is free; all partials are written
         if (tid == 0 && q + 2L * gridDim.x < Q) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(q + 2L * gridDim.x, stage);
         }
-        // column groups 1, 2 -> shared partials [kg-1][mt][r][c][lane]
-        if (kg > 0) {
-#pragma unroll
-            for (int im = 0; im < MPW; im++)
-#pragma unroll
-                for (int r = 0; r < NRHS; r++)
-#pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        const int mt = mg * MPW + im;
-                        const uint32_t o = (uint32_t)((((kg - 1) * P::MT + mt) * NRHS + r) * 4 + c) * 128u + lane * 4u;
-                        asm volatile("st.shared.f32 [%0], %1;" ::"r"(sPART + o), "f"(acc[im][r][c]) : "memory");
-                    }
-        }
-        __syncthreads();
-        if (kg == 0) {
-#pragma unroll
-            for (int im = 0; im < MPW; im++) {
-                const int mt = mg * MPW + im;
+        // warp w < MT adds the column groups' partials of row tile w and stores
+        if (warp < P::MT) {
+            const int mt = warp;
+            {
 #pragma unroll
                 for (int r = 0; r < NRHS; r++) {
                     float y[4];
 #pragma unroll
                     for (int c = 0; c < 4; c++) {
-                        float s = acc[im][r][c];
+                        float s = 0.f;
 #pragma unroll
-                        for (int k = 0; k < P::KG - 1; k++) {
-                            const uint32_t o = (uint32_t)(((k * P::MT + mt) * NRHS + r) * 4 + c) * 128u + lane * 4u;
-                            float p;
-                            asm volatile("ld.shared.f32 %0, [%1];" : "=f"(p) : "r"(sPART + o));
-                            s += p;
-                        }
+                        for (int k = 0; k < P::KG; k++) s += PART[(((k * P::MT + mt) * NRHS + r) * 4 + c) * 32];
                         y[c] = s;
                     }
                     // C: rows g, g+8; columns 2t, 2t+1 (t < 2: Re of v = 2t, 2t+1; t >= 2: Im of v = 2t-4, 2t-3)
