@@ -169,7 +169,7 @@ def run_ours(args, rank, world, local):
     stream = torch.cuda.Stream(dev)
     ctx.set_stream(stream.cuda_stream)
     n = m.nx * m.ny * 3 * m.nz
-    mixed = dict(tol=1e-6, max_outer=5, m_out=30, m_in=10, inner_tol=1e-4, inner_restarts=20)
+    mixed = dict(tol=1e-6, max_outer=5, m_out=30, m_in=10, inner_tol=5e-7, inner_restarts=20)
 
     host_in, host_e0 = [], []
     for f in freqs:

@@ -299,11 +299,18 @@ GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixe
         *true_be = 0;
         return out;
     }
-    apply_dev<double>(ctx, x, t, 1);
-    applies64++;
-    VecOps<double>::sub(b, t, r, n, ctx->stream);
-    ctx->launches++;
-    double rn = norm64(r);
+    // r = b - A x; a zero initial guess needs no complex128 apply
+    double rn;
+    if (norm64(x) == 0) {
+        EGX_CUDA(cudaMemcpyAsync(r, b, n * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
+        rn = bn;
+    } else {
+        apply_dev<double>(ctx, x, t, 1);
+        applies64++;
+        VecOps<double>::sub(b, t, r, n, ctx->stream);
+        ctx->launches++;
+        rn = norm64(r);
+    }
     double be = rn / bn;
     int k = 0;
     bool conv = be < p.tol;

@@ -4,7 +4,8 @@
 // (Extreme.Cartesian.Magnetotellurics/PlaneWaveCalculator.cs:11-83 with the
 // single-lambda recursions of Green/Scalar/Impl/PlanCalculator.cs:173-314).
 // Device: jS = (zeta - zeta0) E0, chi0 = K_chi0 jS, the solve of A chi = chi0
-// from x0 = chi0, Es = (2 sqrt(Re zeta0) chi - jS)/(zeta + conj zeta0) and
+// (complex128 FGMRES from x0 = chi0 as the reference; the mixed solve from zero),
+// Es = (2 sqrt(Re zeta0) chi - jS)/(zeta + conj zeta0) and
 // jQ = Es (zeta - zeta0) + jS (Forward/ForwardSolver.cs:186-436).
 #include <cmath>
 #include <complex>
@@ -224,14 +225,18 @@ int egx_solve_sources(egx_ctx *ctx, egx_green *g, const double *zeta, const doub
         prepare_device(ctx, g, dz, EGX_OP_A);
         for (int i = 0; i < nsrc; i++) {
             double2 *x = xs + (size_t)i * n;
-            EGX_CUDA(cudaMemcpyAsync(x, chi0 + i * n, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
             int applies = 0, refinements = 0;
             double tbe = -1;
             GmresResult r;
             if (p->precision == EGX_PREC_FP64) {
+                // the reference starts FGMRES from chi0 (ForwardSolver.cs:300-306)
+                EGX_CUDA(cudaMemcpyAsync(x, chi0 + i * n, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
                 r = fgmres_dev(ctx, chi0 + i * n, x, p->fgmres, &applies);
                 tbe = r.true_be;
             } else {
+                // the refinement starts from zero: its first residual is chi0
+                // itself, which saves a complex128 apply
+                EGX_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double2), s));
                 r = mixed_dev(ctx, chi0 + i * n, x, p->mixed, &applies, &refinements, &tbe);
             }
             res[i].converged = r.converged;

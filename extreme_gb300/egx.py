@@ -232,7 +232,7 @@ class Context:
             self._check(rc)
         return r.as_dict()
 
-    def mixed_solve(self, b, x0, tol=1e-6, max_outer=10, m_out=30, m_in=10, inner_tol=1e-4, inner_restarts=20):
+    def mixed_solve(self, b, x0, tol=1e-6, max_outer=10, m_out=30, m_in=10, inner_tol=5e-7, inner_restarts=20):
         b = _c128(b)
         x = _c128(x0).copy()
         p = MixedParams(tol, max_outer, m_out, m_in, inner_tol, inner_restarts)
@@ -242,7 +242,7 @@ class Context:
             self._check(rc)
         return x, r.as_dict()
 
-    def mixed_solve_dev(self, b_ptr, x_ptr, tol=1e-6, max_outer=10, m_out=30, m_in=10, inner_tol=1e-4,
+    def mixed_solve_dev(self, b_ptr, x_ptr, tol=1e-6, max_outer=10, m_out=30, m_in=10, inner_tol=5e-7,
                         inner_restarts=20):
         p = MixedParams(tol, max_outer, m_out, m_in, inner_tol, inner_restarts)
         r = Result()
@@ -276,7 +276,7 @@ class Context:
                                      fg.get("max_restarts", 100), fg.get("precond", PRECOND_GMRES),
                                      int(fg.get("check_true", True))),
                          MixedParams(mx.get("tol", 1e-6), mx.get("max_outer", 10), mx.get("m_out", 30),
-                                     mx.get("m_in", 10), mx.get("inner_tol", 1e-4), mx.get("inner_restarts", 20)))
+                                     mx.get("m_in", 10), mx.get("inner_tol", 5e-7), mx.get("inner_restarts", 20)))
         res = (Result * nsrc)()
         if where == DEVICE:
             d = dev_ptrs

@@ -37,7 +37,7 @@ class MixedSettings:
     max_outer: int = 10
     m_out: int = 30
     m_in: int = 10
-    inner_tol: float = 1e-4
+    inner_tol: float = 5e-7
     inner_restarts: int = 20
 
 
