@@ -24,7 +24,7 @@ EXPORTS = [
     "egx_create", "egx_destroy", "egx_last_error", "egx_version", "egx_set_stream", "egx_launch_count",
     "egx_green_build", "egx_green_upload", "egx_green_download", "egx_green_free",
     "egx_op_prepare", "egx_op_apply", "egx_op_apply_c64", "egx_fft2d",
-    "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products",
+    "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products", "egx_dot_products_static",
     "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_read",
 ]
 
@@ -106,6 +106,7 @@ def load(path=None):
     lib.egx_mixed_solve.argtypes = [vp, vp, vp, C.POINTER(MixedParams), C.POINTER(Result), i]
     lib.egx_set_precond.argtypes = [vp, i, PRECOND_FN, vp]
     lib.egx_dot_products.argtypes = [vp, vp, i, vp, C.c_long, vp, i]
+    lib.egx_dot_products_static.argtypes = [vp, vp, i, vp, C.c_long, vp]
     lib.egx_normal_field.argtypes = [C.POINTER(Model), d, vp]
     lib.egx_plane_wave.argtypes = [C.POINTER(Model), d, d, vp, vp]
     lib.egx_solve_sources.argtypes = [vp, vp, vp, vp, vp, vp, vp, i, C.POINTER(SourceParams), vp, vp,
@@ -258,6 +259,13 @@ class Context:
         out = np.empty(Vt.shape[0], np.complex128)
         self._check(self.lib.egx_dot_products(self.h, _ptr(Vt), Vt.shape[0], _ptr(w), w.size, _ptr(out), HOST))
         return out
+
+    def dot_products_static(self, V_ptr, ncols, w_ptr, n, out_ptr):
+        """egx_dot_products_static on device pointers: V holds ncols vectors
+        of n complex128 one after another, out receives ncols complex128.
+        Allocates no device memory (a fixed static scratch, <= 64 columns)."""
+        self._check(self.lib.egx_dot_products_static(self.h, C.c_void_p(V_ptr), ncols, C.c_void_p(w_ptr), n,
+                                                     C.c_void_p(out_ptr)))
 
     def solve_sources(self, green, zeta, zeta0, dz, e0, pols, precision=PREC_FP64, fgmres=None, mixed=None,
                       want_chi=False, where=HOST, dev_ptrs=None):

@@ -161,6 +161,17 @@ int egx_set_precond(egx_ctx *ctx, int kind, egx_precond_fn fn, void *user);
  * conj(V[:, k])^T w for k < ncols, V column-major with leading dimension n. */
 int egx_dot_products(egx_ctx *ctx, const double *V, int ncols, const double *w, long n, double *out, int where);
 
+/* egx_dot_products on device pointers (V, w, out in device memory) that
+ * allocates nothing -- for callers that cannot allocate device memory where
+ * they call it, such as a host whose device memory belongs to its own pool
+ * allocator or code inside a solver callback. No counterpart in the
+ * reference. The partial sums live in one static device array of 128 KiB
+ * that every call on a device shares: at most 64 columns per call (more is
+ * EGX_ERR_INVALID, see egx_last_error); calls that overlap on the GPU race.
+ * The first call on a device looks the array up (cudaGetSymbolAddress) and
+ * should come before any stream capture. */
+int egx_dot_products_static(egx_ctx *ctx, const double *V, int ncols, const double *w, long n, double *out);
+
 /* ---- MT source and the CIE pipeline around the solve ------------------- */
 /* Thickness-averaged 1-D plane-wave field on each anomaly layer
  * (Mt3DForwardSolver.CalculateNormalFieldFromSource, Mt3DForwardSolver.cs:251-275;
