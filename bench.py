@@ -40,9 +40,10 @@ sys.path.insert(0, ROOT)
 METRIC = "MT solves/s to 1e-6 residual (256x256x48): mixed+learned vs plain FP64, 1 GB300"
 
 # DRAM bytes (read + write) of one launch of the complex64 contraction at
-# 256x256x48, from an ncu capture at 128x128x48 scaled by the stored spectral
-# points (the traffic is proportional to them); None until captured.
-CONTRACT_TRAFFIC_BYTES = None
+# 256x256x48: 1.4262 GB measured by ncu at 128x128x48 (16,641 stored points),
+# scaled by the algorithmic bytes (5.6765 GB / 1.4290 GB), which grow with the
+# stored points.
+CONTRACT_TRAFFIC_BYTES = 5.665e9
 
 # Operator applications per polarisation of the reference algorithm
 # (complex128 FGMRES(15) with GMRES(10), tolerance 1e-6) on the 256x256x48
@@ -288,7 +289,7 @@ def run_ours(args, rank, world, local):
                 "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4) if achieved else None, "peak_source": peak_src,
                 "algorithmic_bytes": alg_bytes, "ms_per_launch": round(kms / kc, 4) if kc else None,
-                "traffic": int(CONTRACT_TRAFFIC_BYTES) if CONTRACT_TRAFFIC_BYTES else None}
+                "traffic": int(CONTRACT_TRAFFIC_BYTES) if (m.nx, m.ny, m.nz) == (256, 256, 48) else None}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

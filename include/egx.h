@@ -189,7 +189,8 @@ typedef struct {
 
 /* ForwardSolverGenerics.SolveForOneSource up to jQ for nsrc sources
  * (Forward/ForwardSolverGenerics.cs:30-50, Forward/ForwardSolver.cs:186-436):
- * jS = (zeta - zeta0) E0, chi0 = K_chi0 jS, solve A chi = chi0 from x0 = chi0,
+ * jS = (zeta - zeta0) E0, chi0 = K_chi0 jS, solve A chi = chi0 (EGX_PREC_FP64
+ * from x0 = chi0 as the reference, EGX_PREC_MIXED from zero),
  * Es = (2 sqrt(Re zeta0) chi - jS)/(zeta + conj zeta0), jQ = Es (zeta - zeta0) + jS.
  * e0: [nsrc][nz] complex normal field per layer, pol: [nsrc] component
  * (0 = x, 1 = y); chi (may be NULL), jq: [nsrc][N]; res: [nsrc]. */
