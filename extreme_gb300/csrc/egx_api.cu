@@ -474,9 +474,11 @@ int egx_green_build(egx_ctx *ctx, const egx_model *model, double omega, int n_ha
         g->ny = gm.ny;
         g->nz = gm.nz;
         GreenBuildStats st;
-        build_green(gm, n_hankels, ctx->stream, g->g64, &st, &ctx->launches, &ctx->timers);
+        g->g64.swap(ctx->spare64);  // storage of the last freed tensor, if any
+        build_green(gm, n_hankels, ctx->stream, g->g64, &st, &ctx->launches, &ctx->timers, &ctx->gws);
         if (precision == EGX_PREC_MIXED) {
             GreenDims gd{gm.nx, gm.ny, gm.nz};
+            g->g32.swap(ctx->spare32);
             g->g32.ensure(green_c64_entries(gd) * sizeof(float2));
             green_to_c64(g->g64.as<double2>(), g->g32.as<float2>(), gd, ctx->stream, &ctx->launches);
             g->has32 = true;
@@ -558,6 +560,10 @@ int egx_green_free(egx_ctx *ctx, egx_green *g) {
     }
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    // keep the storage for the next build in this context (a build usually
+    // follows, one frequency after another); egx_destroy releases it
+    if (!ctx->spare64.p) ctx->spare64.swap(g->g64);
+    if (!ctx->spare32.p) ctx->spare32.swap(g->g32);
     delete g;
     return EGX_OK;
 }

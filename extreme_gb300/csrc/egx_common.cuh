@@ -161,6 +161,10 @@ struct DevBuf {
         bytes = n;
     }
     template <typename X> X *as() const { return reinterpret_cast<X *>(p); }
+    void swap(DevBuf &o) {
+        std::swap(p, o.p);
+        std::swap(bytes, o.bytes);
+    }
 };
 
 }  // namespace egx

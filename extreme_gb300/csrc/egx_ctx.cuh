@@ -25,6 +25,10 @@ struct egx_ctx {
     std::string err;
     long launches = 0;
     egx::Timers timers;
+    // Green-tensor build workspace, and the storage of the last freed tensor
+    // (reused by the next build of the same size; released by egx_destroy)
+    egx::GreenWorkspace gws;
+    egx::DevBuf spare64, spare32;
 
     // prepared operator
     egx_green *g = nullptr;

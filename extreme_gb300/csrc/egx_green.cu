@@ -344,7 +344,7 @@ struct Term {
 // written with the parity mirroring into buf[2nx][2ny][tc].
 __global__ void k_cells(const int *__restrict__ rowptr, const Term *__restrict__ terms, const double2 *__restrict__ IA,
                         const double2 *__restrict__ IB, int ntrans, int nseg, int nx, int ny, int t0, int tc, int xs,
-                        int ys, double2 *__restrict__ buf) {
+                        int ys, int compact, double2 *__restrict__ buf) {
     const int cell = blockIdx.x;
     const int i = cell / ny, j = cell - (cell / ny) * ny;
     const int t = blockIdx.y * blockDim.x + threadIdx.x;
@@ -358,6 +358,12 @@ __global__ void k_cells(const int *__restrict__ rowptr, const Term *__restrict__
         acc.y = fma(tm.wa, a.y, acc.y);
         acc.x = fma(tm.wb, b.x, acc.x);
         acc.y = fma(tm.wb, b.y, acc.y);
+    }
+    if (compact) {
+        // quadrant buffer [nx+1][ny+1][tc]: the mirror images are made by
+        // the FFT's loads (fft_lines_sym)
+        buf[((long)i * (ny + 1) + j) * tc + t] = acc;
+        return;
     }
     const int n0 = 2 * nx, n1 = 2 * ny;
     buf[((long)i * n1 + j) * tc + t] = acc;
@@ -374,8 +380,8 @@ __global__ void k_cells(const int *__restrict__ rowptr, const Term *__restrict__
 
 // quad block entry of reference entry tt: packed symmetric entries keep
 // their index, xz/yz entries rc*nz + tr move to rc*(nz+1) + tr.
-__global__ void k_extract(const double2 *__restrict__ buf, int nx, int ny, int tc, int Bs, int off, int t0, int nz,
-                          int asym, double2 *__restrict__ quad) {
+__global__ void k_extract(const double2 *__restrict__ buf, int nx, int ny, int row, int tc, int Bs, int off, int t0,
+                          int nz, int asym, double2 *__restrict__ quad) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     long total = (long)(nx + 1) * (ny + 1) * tc;
     if (idx >= total) return;
@@ -384,7 +390,7 @@ __global__ void k_extract(const double2 *__restrict__ buf, int nx, int ny, int t
     int a = (int)(q / (ny + 1)), b = (int)(q - (long)a * (ny + 1));
     int tt = t0 + t;
     int dst = asym ? (tt / nz) * (nz + 1) + tt % nz : tt;
-    quad[q * Bs + off + dst] = buf[((long)a * 2 * ny + b) * tc + t];
+    quad[q * Bs + off + dst] = buf[((long)a * row + b) * tc + t];
 }
 
 // ---------------------------------------------------------------- host plan
@@ -639,7 +645,7 @@ std::vector<int> background_indices(const GreenModel &m) {
 }
 
 void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &quad, GreenBuildStats *stats,
-                 long *launches, Timers *tm) {
+                 long *launches, Timers *tm, GreenWorkspace *ws) {
     auto t_start = std::chrono::steady_clock::now();
     EGX_CHECK(m.nx > 0 && m.ny > 0 && m.nz > 0 && m.dx > 0 && m.dy > 0, EGX_ERR_INVALID, "bad model dimensions");
     const int L = (int)m.bg_thick.size();
@@ -747,10 +753,21 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
     quad.ensure((size_t)gd.Q() * Bs * sizeof(double2));
     EGX_CUDA(cudaMemsetAsync(quad.p, 0, (size_t)gd.Q() * Bs * sizeof(double2), s));  // row padding stays zero
 
-    DevBuf d_lam, d_lay, d_trans, d_U, d_I, d_rho, d_gidx, d_flags, d_neg, d_radii, d_IA, d_IB, d_rowptr, d_terms,
-        d_buf;
+    GreenWorkspace local_ws;
+    GreenWorkspace &w = ws ? *ws : local_ws;
+    DevBuf &d_lam = w.d_lam, &d_lay = w.d_lay, &d_trans = w.d_trans, &d_U = w.d_U, &d_I = w.d_I, &d_rho = w.d_rho,
+           &d_gidx = w.d_gidx, &d_flags = w.d_flags, &d_neg = w.d_neg, &d_radii = w.d_radii, &d_IA = w.d_IA,
+           &d_IB = w.d_IB, &d_buf = w.d_buf;
+    {
+        std::vector<double> key = {(double)m.nx, (double)m.ny, m.dx, m.dy};
+        key.insert(key.end(), radii.begin(), radii.end());
+        if (key != w.key) {
+            for (bool &c : w.cached) c = false;
+            w.key = key;
+        }
+    }
     FftPlan p0 = make_fft_plan(2 * m.nx), p1 = make_fft_plan(2 * m.ny);
-    DevBuf tw0, tw1;
+    DevBuf &tw0 = w.tw0, &tw1 = w.tw1;
     {
         std::vector<double> t0 = twiddles(2 * m.nx), t1 = twiddles(2 * m.ny);
         dev_upload(tw0, t0, s);
@@ -815,41 +832,67 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
         const int comps_asym[2] = {4, 5}, comps_symm[4] = {0, 1, 2, 3};
         const int *comps = half == 0 ? comps_asym : comps_symm;
         const int ncomp = half == 0 ? 2 : 4;
-        const int blk = half == 0 ? gd.A() : gd.S();
+        // one FFT column per transceiver: nz*nz for xz/yz, nz(nz+1)/2 for the
+        // packed components (k_extract pads the xz/yz rows on the way out)
+        const int blk = ntrans;
+        EGX_CHECK(ntrans == (half == 0 ? m.nz * m.nz : gd.S()), EGX_ERR_INVALID, "transceiver count mismatch");
         const int S = gd.S(), A = gd.A();
         const int offs[6] = {0, S, 2 * S, 3 * S, 4 * S, 4 * S + A};
         const int px[6] = {1, -1, 1, 1, -1, 1}, py[6] = {1, -1, 1, 1, 1, -1};
-        const long cells4 = 4L * m.nx * m.ny;
+        // compact: the real-space quadrant only, its mirror images generated
+        // by the FFT's loads (half the y lines, a quarter of the memory);
+        // otherwise the full 2nx x 2ny grid populated by mirroring
+        const int n0 = 2 * m.nx, n1 = 2 * m.ny;
+        const bool compact = fft_lines_sym_ok(n0) && fft_lines_sym_ok(n1);
+        const long cells4 = compact ? (long)(m.nx + 1) * (m.ny + 1) : 4L * m.nx * m.ny;
+        const int row = compact ? m.ny + 1 : n1;
         int tc = (int)std::min<long>(blk, std::max<long>(1, (long)(1.5e9 / (cells4 * sizeof(double2)))));
         d_buf.ensure((size_t)cells4 * tc * sizeof(double2));
         for (int ci = 0; ci < ncomp; ci++) {
             const int c = comps[ci];
             auto t_int = std::chrono::steady_clock::now();
-            std::vector<int> rowptr;
-            std::vector<Term> terms;
-            cell_terms(m, radii, c, slot, rowptr, terms);
-            if (stats) stats->face_terms += (long)terms.size();
-            int *drow = dev_upload(d_rowptr, rowptr, s);
-            Term *dterm = dev_upload(d_terms, terms, s);
+            if (!w.cached[c]) {
+                // the term lists depend on the lateral mesh and radii only:
+                // made once and reused for every frequency of the model
+                std::vector<int> rowptr;
+                std::vector<Term> terms;
+                cell_terms(m, radii, c, slot, rowptr, terms);
+                dev_upload(w.rowptr[c], rowptr, s);
+                dev_upload(w.terms[c], terms, s);
+                EGX_CUDA(cudaStreamSynchronize(s));
+                w.nterms[c] = (long)terms.size();
+                w.cached[c] = true;
+            }
+            if (stats) stats->face_terms += w.nterms[c];
+            const int *drow = w.rowptr[c].as<int>();
+            const Term *dterm = w.terms[c].as<Term>();
             for (int t0 = 0; t0 < blk; t0 += tc) {
                 const int tcc = std::min(tc, blk - t0);
-                EGX_CUDA(cudaMemsetAsync(d_buf.p, 0, (size_t)cells4 * tcc * sizeof(double2), s));
+                if (!compact) EGX_CUDA(cudaMemsetAsync(d_buf.p, 0, (size_t)cells4 * tcc * sizeof(double2), s));
                 dim3 grid(m.nx * m.ny, (tcc + 127) / 128);
                 int ev = tm ? tm->begin(EGX_K_GREEN_CELLS, s) : -1;
                 k_cells<<<grid, 128, 0, s>>>(drow, dterm, d_IA.as<double2>(), d_IB.as<double2>(), ntrans, nseg, m.nx,
-                                             m.ny, t0, tcc, px[c], py[c], d_buf.as<double2>());
+                                             m.ny, t0, tcc, px[c], py[c], compact ? 1 : 0, d_buf.as<double2>());
                 if (tm) tm->end(ev, s);
                 EGX_CUDA(cudaGetLastError());
                 ev = tm ? tm->begin(EGX_K_GREEN_FFT, s) : -1;
-                // y along all 2nx rows; x along ky <= ny, kx <= nx kept
-                const int n0 = 2 * m.nx, n1 = 2 * m.ny;
-                fft_lines<double>(d_buf.as<double2>(), n0, (long)n1 * tcc, tcc, tcc, n1, n1, p1, tw1.as<double2>(), -1,
-                                  s, launches);
-                fft_lines<double>(d_buf.as<double2>(), m.ny + 1, tcc, (long)n1 * tcc, tcc, n0, m.nx + 1, p0,
-                                  tw0.as<double2>(), -1, s, launches);
+                if (compact) {
+                    // y along the nx computed rows, ky <= ny kept; then x along
+                    // ky <= ny, kx <= nx kept (row nx of the input is zero)
+                    fft_lines_sym<double>(d_buf.as<double2>(), m.nx, (long)row * tcc, tcc, tcc, py[c], m.ny + 1, n1,
+                                          tw1.as<double2>(), -1, s, launches);
+                    fft_lines_sym<double>(d_buf.as<double2>(), m.ny + 1, tcc, (long)row * tcc, tcc, px[c], m.nx + 1,
+                                          n0, tw0.as<double2>(), -1, s, launches);
+                } else {
+                    // y along all 2nx rows; x along ky <= ny, kx <= nx kept
+                    fft_lines<double>(d_buf.as<double2>(), n0, (long)n1 * tcc, tcc, tcc, n1, n1, p1,
+                                      tw1.as<double2>(), -1, s, launches);
+                    fft_lines<double>(d_buf.as<double2>(), m.ny + 1, tcc, (long)n1 * tcc, tcc, n0, m.nx + 1, p0,
+                                      tw0.as<double2>(), -1, s, launches);
+                }
                 if (tm) tm->end(ev, s);
                 long n = (long)(m.nx + 1) * (m.ny + 1) * tcc;
-                k_extract<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_buf.as<double2>(), m.nx, m.ny, tcc, Bs,
+                k_extract<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_buf.as<double2>(), m.nx, m.ny, row, tcc, Bs,
                                                                       offs[c], t0, m.nz, c >= 4 ? 1 : 0,
                                                                       quad.as<double2>());
                 EGX_CUDA(cudaGetLastError());

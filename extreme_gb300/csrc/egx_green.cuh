@@ -27,10 +27,21 @@ struct GreenBuildStats {
     double ms_scalars = 0, ms_integrate = 0, ms_fft = 0;
 };
 
+// Device workspace of build_green that a context keeps across builds: the
+// scratch buffers, and per component the face-integration term lists (CSR),
+// which depend only on the lateral mesh and the radii -- not on frequency.
+struct GreenWorkspace {
+    DevBuf d_lam, d_lay, d_trans, d_U, d_I, d_rho, d_gidx, d_flags, d_neg, d_radii, d_IA, d_IB, d_buf, tw0, tw1;
+    std::vector<double> key;  // nx, ny, dx, dy and the radii of the cached term lists
+    DevBuf rowptr[6], terms[6];
+    long nterms[6] = {};
+    bool cached[6] = {};
+};
+
 // Build the spectral tensor into `quad` (device, complex128, layout of
 // GreenDims: quadrant points x [xx|xy|yy|zz|xz|yz] blocks).
 void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &quad, GreenBuildStats *stats,
-                 long *launches, Timers *timers = nullptr);
+                 long *launches, Timers *timers = nullptr, GreenWorkspace *ws = nullptr);
 
 // Index of the background layer holding each anomaly layer; throws
 // EGX_ERR_MODEL when a layer straddles an interface (ModelUtils.cs:160-185).

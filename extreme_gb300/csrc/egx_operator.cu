@@ -191,6 +191,30 @@ __global__ void __launch_bounds__(reg_threads<N, T>())
     fft_reg<T, N>(reinterpret_cast<C<T> *>(smem_raw), tw, +1, load, store);
 }
 
+// Lines whose second half is the parity image of the first: element e of a
+// line is v[e] for e < N/2, 0 at e = N/2 and par * v[N - e] beyond, with only
+// v[0 .. N/2) stored; outputs e < nstore are written back in place.
+template <typename T, int N>
+__global__ void __launch_bounds__(reg_threads<N, T>())
+    k_lines_sym_r(C<T> *buf, long lstride, long estride, int B, T par, int nstore, const C<T> *__restrict__ tw,
+                  int sign) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int BT = RegCols<T>::BT, NH = N / 2;
+    const int b = blockIdx.y * BT + (int)(threadIdx.x % BT);
+    const bool bok = b < B;
+    C<T> *line = buf + (long)blockIdx.x * lstride + b;
+    auto load = [&](int e) -> C<T> {
+        if (!bok || e == NH) return mk<T>(0, 0);
+        if (e < NH) return line[e * estride];
+        const C<T> v = line[(N - e) * estride];
+        return mk<T>(par * v.x, par * v.y);
+    };
+    auto store = [&](int e, C<T> v) {
+        if (bok && e < nstore) line[e * estride] = v;
+    };
+    fft_reg<T, N>(reinterpret_cast<C<T> *>(smem_raw), tw, sign, load, store);
+}
+
 template <typename T, int N>
 static void reg_attr(const void *fn) {
     constexpr size_t sm = reg_smem<N, T>();
@@ -455,6 +479,36 @@ void fft_lines(C<T> *buf, int nlines, long lstride, long estride, int B, int nlo
     EGX_CUDA(cudaGetLastError());
     if (launches) *launches += 1;
 }
+
+template <typename T, int N>
+static void launch_sym(dim3 grid, cudaStream_t s, C<T> *buf, long lstride, long estride, int B, T par, int nstore,
+                       const C<T> *tw, int sign) {
+    static bool a = false;
+    if (!a) reg_attr<T, N>((const void *)k_lines_sym_r<T, N>), a = true;
+    k_lines_sym_r<T, N><<<grid, reg_threads<N, T>(), reg_smem<N, T>(), s>>>(buf, lstride, estride, B, par, nstore, tw,
+                                                                            sign);
+}
+
+bool fft_lines_sym_ok(int n) { return reg_fft_ok(n); }
+
+template <typename T>
+void fft_lines_sym(C<T> *buf, int nlines, long lstride, long estride, int B, int parity, int nstore, int n,
+                   const C<T> *tw, int sign, cudaStream_t s, long *launches) {
+    EGX_CHECK(reg_fft_ok(n), EGX_ERR_INVALID, "mirrored FFT lines need a length in {64, 128, 256, 512}");
+    dim3 grid(nlines, (B + RegCols<T>::BT - 1) / RegCols<T>::BT);
+    const T par = (T)parity;
+    switch (n) {
+        case 64: launch_sym<T, 64>(grid, s, buf, lstride, estride, B, par, nstore, tw, sign); break;
+        case 128: launch_sym<T, 128>(grid, s, buf, lstride, estride, B, par, nstore, tw, sign); break;
+        case 256: launch_sym<T, 256>(grid, s, buf, lstride, estride, B, par, nstore, tw, sign); break;
+        default: launch_sym<T, 512>(grid, s, buf, lstride, estride, B, par, nstore, tw, sign); break;
+    }
+    EGX_CUDA(cudaGetLastError());
+    if (launches) *launches += 1;
+}
+
+template void fft_lines_sym<double>(C<double> *, int, long, long, int, int, int, int, const C<double> *, int,
+                                    cudaStream_t, long *);
 
 template void fft_lines<double>(C<double> *, int, long, long, int, int, int, const FftPlan &, const C<double> *, int,
                                 cudaStream_t, long *);

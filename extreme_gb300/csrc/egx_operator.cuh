@@ -69,6 +69,15 @@ template <typename T>
 void fft_lines(C<T> *buf, int nlines, long lstride, long estride, int B, int nload, int nstore, const FftPlan &p,
                const C<T> *tw, int sign, cudaStream_t s, long *launches);
 
+// DFTs of length n of lines stored by their first half: element e is
+// v[e] for e < n/2, 0 at n/2 and parity * v[n - e] beyond (a real-space
+// Green component and its mirror image); outputs e < nstore are written back
+// in place. Lengths with a register plan only (fft_lines_sym_ok).
+bool fft_lines_sym_ok(int n);
+template <typename T>
+void fft_lines_sym(C<T> *buf, int nlines, long lstride, long estride, int B, int parity, int nstore, int n,
+                   const C<T> *tw, int sign, cudaStream_t s, long *launches);
+
 // In-place batched 2-D DFT (egx_fft2d).
 template <typename T>
 void fft2d(C<T> *buf, int n0, int n1, int howmany, int sign, const C<T> *tw0, const C<T> *tw1, const FftPlan &p0,

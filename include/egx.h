@@ -127,6 +127,9 @@ int egx_green_upload(egx_ctx *ctx, int nx, int ny, int nz, const double *const c
                      int precision, egx_green **out);
 /* Download the complex128 spectral tensor in the reference layout. */
 int egx_green_download(egx_ctx *ctx, const egx_green *g, double *const comps[6]);
+/* Free a tensor. The context keeps its device storage for the next
+ * egx_green_build (one frequency after another reuses it); egx_destroy
+ * releases it. */
 int egx_green_free(egx_ctx *ctx, egx_green *g);
 
 /* ---- operator (ConvolutionOperator) ------------------------------------ */
