@@ -50,17 +50,6 @@ void upload_twiddles(DevBuf &dst, int n, cudaStream_t s) {
     EGX_CUDA(cudaStreamSynchronize(s));
 }
 
-void ensure_twiddles(egx_ctx *ctx, int n0, int n1) {
-    if (ctx->tw_n0 == n0 && ctx->tw_n1 == n1) return;
-    ctx->p0 = make_fft_plan(n0);
-    ctx->p1 = make_fft_plan(n1);
-    upload_twiddles<double>(ctx->tw0_64, n0, ctx->stream);
-    upload_twiddles<double>(ctx->tw1_64, n1, ctx->stream);
-    upload_twiddles<float>(ctx->tw0_32, n0, ctx->stream);
-    upload_twiddles<float>(ctx->tw1_32, n1, ctx->stream);
-    ctx->tw_n0 = n0;
-    ctx->tw_n1 = n1;
-}
 
 // r = (zeta - zeta0)/(zeta + conj zeta0) (A) or sqrt(Re zeta0)/(zeta + conj zeta0)
 // (Chi0) (ConvolutionOperator.PrepareRFunction, ConvolutionOperator.cs:113-143).
@@ -162,6 +151,34 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
 }
 
 }  // namespace
+
+GreenModel green_model(const egx_model *model, double omega) {
+    GreenModel gm;
+    gm.nx = model->nx;
+    gm.ny = model->ny;
+    gm.nz = model->nz;
+    gm.dx = model->dx;
+    gm.dy = model->dy;
+    gm.depth.assign(model->layer_depth, model->layer_depth + model->nz);
+    gm.thick.assign(model->layer_thickness, model->layer_thickness + model->nz);
+    gm.bg_thick.assign(model->bg_thickness, model->bg_thickness + model->n_bg);
+    gm.bg_sigma.assign(model->bg_sigma, model->bg_sigma + model->n_bg);
+    gm.zero_air_level = model->zero_air_level;
+    gm.omega = omega;
+    return gm;
+}
+
+void ensure_twiddles(egx_ctx *ctx, int n0, int n1) {
+    if (ctx->tw_n0 == n0 && ctx->tw_n1 == n1) return;
+    ctx->p0 = make_fft_plan(n0);
+    ctx->p1 = make_fft_plan(n1);
+    upload_twiddles<double>(ctx->tw0_64, n0, ctx->stream);
+    upload_twiddles<double>(ctx->tw1_64, n1, ctx->stream);
+    upload_twiddles<float>(ctx->tw0_32, n0, ctx->stream);
+    upload_twiddles<float>(ctx->tw1_32, n1, ctx->stream);
+    ctx->tw_n0 = n0;
+    ctx->tw_n1 = n1;
+}
 
 void upload_model(egx_ctx *ctx, egx_green *g, const double *zeta, const double *zeta0, int where) {
     const long ncell = (long)g->nx * g->ny;
@@ -457,18 +474,7 @@ int egx_green_build(egx_ctx *ctx, const egx_model *model, double omega, int n_ha
                   EGX_ERR_INVALID, "null model arrays");
         EGX_CHECK(omega > 0, EGX_ERR_INVALID, "omega must be positive");
         set_device(ctx);
-        GreenModel gm;
-        gm.nx = model->nx;
-        gm.ny = model->ny;
-        gm.nz = model->nz;
-        gm.dx = model->dx;
-        gm.dy = model->dy;
-        gm.depth.assign(model->layer_depth, model->layer_depth + model->nz);
-        gm.thick.assign(model->layer_thickness, model->layer_thickness + model->nz);
-        gm.bg_thick.assign(model->bg_thickness, model->bg_thickness + model->n_bg);
-        gm.bg_sigma.assign(model->bg_sigma, model->bg_sigma + model->n_bg);
-        gm.zero_air_level = model->zero_air_level;
-        gm.omega = omega;
+        GreenModel gm = green_model(model, omega);
         auto g = std::unique_ptr<egx_green>(new egx_green());
         g->nx = gm.nx;
         g->ny = gm.ny;

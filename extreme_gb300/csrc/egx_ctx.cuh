@@ -56,6 +56,8 @@ struct egx_ctx {
     egx::DevBuf js, chi0;
     egx::DevBuf errflag;  // device int: EGX_ERR_TIMEOUT from a bounded wait
     egx::GreenBuildStats last_build;
+    // observation level: E and H level tensors, transformed sources, 3-column results
+    egx::DevBuf lvl_g[2], lvl_x, lvl_out, lvl_in, lvl_field;
 };
 
 namespace egx {
@@ -72,6 +74,10 @@ GmresResult fgmres_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_gmr
 GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixed_params &p, int *applies,
                       int *refinements, double *true_be);
 int fail(egx_ctx *ctx, int code, const std::string &msg);
+// egx_model -> the build's model at angular frequency omega
+GreenModel green_model(const egx_model *model, double omega);
+// FFT plans and twiddles of lengths n0 (x) and n1 (y) in ctx
+void ensure_twiddles(egx_ctx *ctx, int n0, int n1);
 // Throws EGX_ERR_TIMEOUT (and clears the flag) if a kernel gave up a bounded
 // wait; call after a stream synchronisation.
 void check_device_error(egx_ctx *ctx);

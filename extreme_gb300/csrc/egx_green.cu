@@ -290,7 +290,7 @@ __global__ void k_kernels(const double *__restrict__ lam, int nl, const double2 
 // I[u][trans][g] = norm * sum_j h[430 - j] * U[u][trans][col0 + i + j]
 __global__ void k_hankel(const double2 *__restrict__ U, int nu, int ntrans, long nl_total, long col0, int nrho,
                          const double *__restrict__ rho, const int *__restrict__ gidx, const int *__restrict__ use_h0,
-                         const int *__restrict__ negate, double2 *__restrict__ I, int nrad) {
+                         const int *__restrict__ negate, double2 *__restrict__ I, int nrad, double den_scale) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)nu * ntrans * nrho) return;
     int i = (int)(idx % nrho);
@@ -306,7 +306,7 @@ __global__ void k_hankel(const double2 *__restrict__ U, int nu, int ntrans, long
         sx += v.x * hj;
         sy += v.y * hj;
     }
-    double den = 2.0 * M_PI * rho[i];
+    double den = den_scale * rho[i];   // 2 pi (E scalars) or 4 pi (H scalars)
     if (negate[u]) {
         sx = -sx;
         sy = -sy;
@@ -617,6 +617,331 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// ---------------------------------------------------------------- observation level
+// Volume-to-point kernels U of one mode (VolumeToPointCalculatorU.cs:21-352):
+// the receiver is the point zw = T0.r1, the transmitter the layer [s1, s2].
+struct VtpTerms {
+    double2 T, R, psi15, psi34, psi5;
+};
+
+__device__ VtpTerms vtp_terms(const double2 *Eta, const double2 *P, const double2 *Q, long nl, int m, const LayerArgs &a,
+                              const Trans &T0, double lam) {
+#define E(k) Eta[(long)(k) * nl + m]
+    const int r = T0.r, s = T0.s, t = min(r, s), b = max(r, s);
+    const double zw = T0.r1, z1 = T0.s1, z2 = T0.s2;
+    const double dt = a.tops[t], db1 = a.tops[b + 1];
+    const double2 er = E(r), es = E(s), et = E(t), eb = E(b);
+    auto ex3 = [](double c1, double2 v1, double c2, double2 v2, double c3, double2 v3) {
+        return dexp(dadd(dadd(dscal(c1, v1), dscal(c2, v2)), dscal(c3, v3)));
+    };
+    VtpTerms o;
+    // CalculateT / CalculateR with (z1, z2, r, s)
+    o.T = dsub(ex3(-zw, er, -z1, es, 2 * dt, et), ex3(-zw, er, -z2, es, 2 * dt, et));
+    o.R = dsub(ex3(-2 * db1, eb, z2, es, zw, er), ex3(-2 * db1, eb, z1, es, zw, er));
+    const double2 pt = P[(long)t * nl + m], qb = Q[(long)b * nl + m];
+    const double2 F = dadd(dscal(-2 * db1, eb), dscal(2 * dt, et));
+    if (T0.kase == 0) {
+        // CalcPsi1RcAndTrMatch / CalcPsi3And4RcAndTrMatch / CalcPsi5RcAndTrMatch, n = r = s
+        const int n = r;
+        const double2 en = E(n);
+        const double2 Fn = dadd(dscal(-2 * a.tops[n + 1], en), dscal(2 * a.tops[n], en));
+        auto ctop = [&](double x1, double x2) { return dsub(dexp(dscal(zw - x1, en)), dexp(dscal(zw - x2, en))); };
+        auto cbot = [&](double x1, double x2) { return dsub(dexp(dscal(x2 - zw, en)), dexp(dscal(x1 - zw, en))); };
+        auto dtop = [&](double x1, double x2) {
+            return dsub(dexp(dadd(Fn, dscal(x2 - zw, en))), dexp(dadd(Fn, dscal(x1 - zw, en))));
+        };
+        auto dbot = [&](double x1, double x2) {
+            return dsub(dexp(dadd(Fn, dscal(zw - x1, en))), dexp(dadd(Fn, dscal(zw - x2, en))));
+        };
+        const double2 pq = dmul(P[(long)n * nl + m], Q[(long)n * nl + m]);
+        o.psi15 = dadd(dadd(ctop(zw, z2), cbot(z1, zw)), dmul(pq, dadd(dtop(zw, z2), dbot(z1, zw))));
+        o.psi34 = dadd(dsub(ctop(zw, z2), cbot(z1, zw)), dmul(pq, dadd(dneg(dtop(zw, z2)), dtop(z1, zw))));
+        const double ln = a.thick[n];
+        const double2 kk = dmk(-a.omega * kMu0 * a.zeta[n].y, a.omega * kMu0 * a.zeta[n].x);
+        double2 v = dmul(pq, dadd(dexp(dscal(-(2 * ln - (z2 - zw)), en)), dexp(dscal(-(2 * ln - (zw - z1)), en))));
+        v = dsub(v, dadd(dexp(dscal(-(z2 - zw), en)), dexp(dscal(-(zw - z1), en))));
+        const double2 w = dsub(dmk(1, 0), dmul(pq, dexp(dscal(-2 * ln, en))));
+        o.psi5 = dadd(v, dscal(2.0 / (lam * lam), dmul(kk, w)));
+    } else if (T0.kase == 2) {
+        // receiver above: CTop, DTop with (z1, z2, r, s)
+        const double2 C = dsub(dexp(dadd(dscal(-z1, es), dscal(zw, er))), dexp(dadd(dscal(-z2, es), dscal(zw, er))));
+        const double2 D = dsub(dexp(dadd(F, dadd(dscal(z2, es), dscal(-zw, er)))),
+                               dexp(dadd(F, dadd(dscal(z1, es), dscal(-zw, er)))));
+        const double2 pqd = dmul(dmul(pt, qb), D);
+        o.psi15 = dadd(C, pqd);
+        o.psi34 = dsub(C, pqd);
+        o.psi5 = o.psi15;
+    } else {
+        // receiver below: CBot, DBot with (z1, z2, r, s)
+        const double2 C = dsub(dexp(dadd(dscal(-zw, er), dscal(z2, es))), dexp(dadd(dscal(-zw, er), dscal(z1, es))));
+        const double2 D = dsub(dexp(dadd(F, dadd(dscal(-z1, es), dscal(zw, er)))),
+                               dexp(dadd(F, dadd(dscal(-z2, es), dscal(zw, er)))));
+        const double2 pqd = dmul(dmul(pt, qb), D);
+        o.psi15 = dadd(C, pqd);
+        o.psi34 = dadd(dneg(C), pqd);
+        o.psi5 = o.psi15;
+    }
+#undef E
+    return o;
+}
+
+// Per (transceiver, lambda): the pre-Hankel kernels of the level scalars
+// (PlanCalculator.CalculateForE/H, PlanCalculator.cs:60-140, with
+// NormalizeBeforeHankelForE/H, ScalarMathUtils.cs:171-263).
+//   E (kind 0): slots I1..I5 = U1(1) i omega mu0/2, U2(s)/2zr, U3(s) lam/2zr,
+//               -U4(s) lam/2zr, U5(s) lam^2/2zr;
+//   H (kind 1): slots I1..I4 = U3(1), U4(s), U1(s) lam, U1(1) lam
+// ("1": the P1/Q1/A1 mode, "s": the sigma mode).
+__global__ void k_kernels_vtp(const double *__restrict__ lam, int nl, const double2 *__restrict__ lay,
+                              const LayerArgs a, const Trans *__restrict__ trans, int ntrans, int kind,
+                              double2 *__restrict__ U, long nl_total, long col0) {
+    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)ntrans * nl) return;
+    const int tr = (int)(idx / nl);
+    const int m = (int)(idx - (long)tr * nl);
+    const Trans T0 = trans[tr];
+    const int L = a.L;
+    const double2 *Eta = lay, *Ex = lay + (long)L * nl, *P1 = lay + 2L * L * nl, *Q1 = lay + 3L * L * nl;
+    const double2 *Ps = lay + 4L * L * nl, *Qs = lay + 5L * L * nl;
+    const int r = T0.r, s = T0.s, t = min(r, s), b = max(r, s);
+    const double l = lam[m];
+    auto E = [&](int k) { return Eta[(long)k * nl + m]; };
+    auto chain = [&](const double2 *P, const double2 *Q) {
+        double2 A = drecip(dmul(E(b), dsub(dmk(1, 0), dmul(dmul(P[(long)b * nl + m], Q[(long)b * nl + m]),
+                                                             Ex[(long)b * nl + m]))));
+        for (int k = b - 1; k >= t; k--) {
+            double2 num = dadd(dmk(1, 0), P[(long)(k + 1) * nl + m]);
+            double2 den = dadd(dmk(1, 0), dmul(P[(long)k * nl + m], Ex[(long)k * nl + m]));
+            A = dmul(dmul(ddiv(num, den), dexp(dscal(a.tops[k + 1], dsub(E(k + 1), E(k))))), A);
+        }
+        return A;
+    };
+    const double2 er = E(r), es = E(s);
+    const double2 a1 = chain(P1, Q1);
+    double2 as = chain(Ps, Qs);
+    if (r > s) as = dmul(ddiv(a.zeta[r], a.zeta[s]), as);
+    const VtpTerms v1 = vtp_terms(Eta, P1, Q1, nl, m, a, T0, l);
+    const VtpTerms vs = vtp_terms(Eta, Ps, Qs, nl, m, a, T0, l);
+    auto pre = [&](const double2 *P, const double2 *Q, const VtpTerms &v, double psign) {
+        return dadd(dmul(dscal(psign, P[(long)t * nl + m]), v.T), dmul(Q[(long)b * nl + m], v.R));
+    };
+    auto u1 = [&](const double2 *P, const double2 *Q, const VtpTerms &v, double2 A) {
+        return dmul(ddiv(A, es), dadd(pre(P, Q, v, 1), v.psi15));
+    };
+    auto u3 = [&](const double2 *P, const double2 *Q, const VtpTerms &v, double2 A) {
+        return dmul(dmul(A, ddiv(er, es)), dadd(pre(P, Q, v, -1), v.psi34));
+    };
+    auto u4 = [&](const double2 *P, const double2 *Q, const VtpTerms &v, double2 A) {
+        return dmul(A, dsub(pre(P, Q, v, -1), v.psi34));
+    };
+    double2 *Ub = U + (long)tr * nl_total + col0 + m;
+    const long us = (long)ntrans * nl_total;
+    if (kind == 0) {
+        const double2 zr2 = dscal(2.0, a.zeta[r]);
+        Ub[0] = dmul(u1(P1, Q1, v1, a1), dmk(0.0, a.omega * kMu0 * 0.5));
+        Ub[us] = ddiv(dmul(dmul(as, er), dsub(pre(Ps, Qs, vs, 1), vs.psi15)), zr2);
+        Ub[2 * us] = dmul(u3(Ps, Qs, vs, as), ddiv(dmk(l, 0), zr2));
+        Ub[3 * us] = dmul(u4(Ps, Qs, vs, as), ddiv(dmk(-l, 0), zr2));
+        const double2 u5 = dmul(ddiv(as, es), dadd(pre(Ps, Qs, vs, 1), vs.psi5));
+        Ub[4 * us] = dmul(u5, ddiv(dmk(l * l, 0), zr2));
+    } else {
+        Ub[0] = u3(P1, Q1, v1, a1);
+        Ub[us] = u4(Ps, Qs, vs, as);
+        Ub[2 * us] = dscal(l, u1(Ps, Qs, vs, as));
+        Ub[3 * us] = dscal(l, u1(P1, Q1, v1, a1));
+    }
+}
+
+// Zero radius of the first plan item (ScalarMathUtils.CalculateZeroRhoFor{E,H},
+// ScalarMathUtils.cs:33-87): I3 and I4 extrapolated from the item's second
+// and third radii, the others 0. I[u][trans][nrad], radius 0 at index 0.
+__global__ void k_zero_rho(double2 *__restrict__ I, int nu, int ntrans, int nrad, int g1, int g2, double a2) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nu * ntrans) return;
+    const int u = idx / ntrans;
+    double2 *v = I + (long)idx * nrad;
+    if (u == 2 || u == 3) {
+        const double2 f1 = v[g1], f2 = v[g2];
+        v[0] = dmk((f1.x * a2 - f2.x) / (a2 - 1), (f1.y * a2 - f2.y) / (a2 - 1));
+    } else {
+        v[0] = dmk(0, 0);
+    }
+}
+
+// Level tensor value of every cell of the full 2nx x 2ny offset grid for
+// transmitter layers [0, nt): buf[cell][nt] (cells without terms stay 0).
+__global__ void k_cells_level(const int *__restrict__ rowptr, const Term *__restrict__ terms,
+                              const double2 *__restrict__ IA, const double2 *__restrict__ IB, int ntrans, int nseg,
+                              int ncell, double2 *__restrict__ buf) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)ncell * ntrans) return;
+    const int cell = (int)(idx / ntrans), t = (int)(idx - (long)cell * ntrans);
+    double2 acc = dmk(0, 0);
+    for (int e = rowptr[cell]; e < rowptr[cell + 1]; e++) {
+        const Term tm = terms[e];
+        const long o = ((long)tm.src * nseg + tm.seg) * ntrans + t;
+        const double2 a = IA[o], b = IB[o];
+        acc.x = fma(tm.wa, a.x, fma(tm.wb, b.x, acc.x));
+        acc.y = fma(tm.wa, a.y, fma(tm.wb, b.y, acc.y));
+    }
+    buf[idx] = acc;
+}
+
+// Component tables of the level tensors, in the order of level_components:
+// E: xx yy zz xy xz yz zx zy; H: xx yx xy xz yz zx zy. QSigns (QSign.cs:31-39)
+// and (integral factor, scalar) of AddToQBuffAlong{X,Y}{Electric,Magnetic}
+// (GreenTensorCalculator.cs:505-552); 0 = not filled in that direction.
+const int kLvQX[2][8] = {{1, -1, -1, -1, 1, 1, 1, 1}, {-1, 1, -1, 1, 1, 1, 1, 0}};
+const int kLvQY[2][8] = {{-1, 1, -1, -1, 1, 1, 1, 1}, {-1, -1, 1, 1, 1, 1, 1, 0}};
+const int kLvQXS[2][8] = {{1, -1, -1, 1, -1, 1, -1, 1}, {1, 1, -1, 1, -1, 1, -1, 0}};
+const int kLvQYS[2][8] = {{-1, 1, -1, 1, 1, -1, 1, -1}, {1, -1, 1, 1, 1, -1, 1, 0}};
+const int kLvFacX[2][8] = {{2, 2, 2, 3, 0, 1, 0, 1}, {3, 2, 2, 1, 0, 1, 0, 0}};
+const int kLvSrcX[2][8] = {{1, 2, 5, 2, 0, 3, 0, 4}, {2, 1, 2, 3, 0, 4, 0, 0}};
+const int kLvFacY[2][8] = {{2, 2, 2, 3, 1, 0, 1, 0}, {3, 2, 2, 0, 1, 0, 1, 0}};
+const int kLvSrcY[2][8] = {{2, 1, 5, 1, 3, 0, 4, 0}, {1, 2, 1, 0, 3, 0, 4, 0}};
+
+// Term lists of all components of a level tensor over the full offset grid
+// (AtoOLevelGreenTensorCalculator.cs:82-126 with GreenTensorCalculator.cs:166-437):
+// knots at x = dx (i - 1/2) + shift_x, i in [-nx+1, nx], y likewise; cell
+// (i, j) is row ((i < 0 ? 2nx + i : i) * 2ny + (j < 0 ? 2ny + j : j)). The
+// face integrations are made once and shared by the components.
+void level_terms(const GreenModel &m, const std::vector<double> &radii, double shx, double shy, int kind, int ncomp,
+                 std::vector<std::vector<int>> &rowptr, std::vector<std::vector<Term>> &terms) {
+    const int nx = m.nx, ny = m.ny, lx = -nx + 1, rx = nx, ly = -ny + 1, ry = ny;
+    const double dx = m.dx, dy = m.dy;
+    auto X = [&](int i) { return dx * (i - 0.5) + shx; };
+    auto Y = [&](int j) { return dy * (j - 0.5) + shy; };
+    const int w = ry - ly + 1;
+    std::vector<Knot> kn((size_t)(rx - lx + 1) * w);
+    for (int i = lx; i <= rx; i++)
+        for (int j = ly; j <= ry; j++) kn[(size_t)(i - lx) * w + (j - ly)] = make_knot(radii, X(i), Y(j));
+    std::vector<Knot> zx(w), zy(rx - lx + 1);
+    for (int j = ly; j <= ry; j++) zx[j - ly] = make_knot(radii, 0.0, Y(j));
+    for (int i = lx; i <= rx; i++) zy[i - lx] = make_knot(radii, X(i), 0.0);
+    auto K = [&](int i, int j) { return kn[(size_t)(i - lx) * w + (j - ly)]; };
+    auto row = [&](int i, int j) { return (int)((i < 0 ? 2 * nx + i : i) * (2 * ny) + (j < 0 ? 2 * ny + j : j)); };
+    // events: one face integration (parts [p0, p0 + np)) added to 1 or 2 cells
+    struct Ev {
+        int dir, symm, ncell, cell[2], sign[2], p0, np;
+    };
+    std::vector<Ev> evs;
+    std::vector<SegF> all, parts;
+    auto push = [&](int dir, bool symm, int i, int j) {
+        Ev e{dir, symm ? 1 : 0, 0, {0, 0}, {0, 0}, (int)all.size(), (int)parts.size()};
+        const int lo = dir == 0 ? ly : lx, hi = dir == 0 ? ry : rx, v = dir == 0 ? j : i;
+        auto cell = [&](int a, int b) { return dir == 0 ? row(i, b) : row(a, j); };
+        if (v == lo) {
+            e.cell[0] = dir == 0 ? cell(0, lo) : cell(lo, 0);
+            e.sign[0] = -1;
+            e.ncell = 1;
+        } else if (v == hi) {
+            e.cell[0] = dir == 0 ? cell(0, hi - 1) : cell(hi - 1, 0);
+            e.sign[0] = 1;
+            e.ncell = 1;
+        } else {
+            e.cell[0] = dir == 0 ? cell(0, v - 1) : cell(v - 1, 0);
+            e.sign[0] = 1;
+            e.cell[1] = dir == 0 ? cell(0, v) : cell(v, 0);
+            e.sign[1] = -1;
+            e.ncell = 2;
+        }
+        all.insert(all.end(), parts.begin(), parts.end());
+        evs.push_back(e);
+    };
+    for (int j = ly; j <= ry; j++) {
+        const double y = Y(j);
+        for (int i = lx; i < rx; i++) {
+            const double x1 = X(i), x2 = X(i + 1);
+            if (x1 > 0 && x2 > 0) {
+                integrate(radii, K(i, j), K(i + 1, j), x1, x2, y, parts);
+                push(0, false, i, j);
+            } else if (x1 < 0 && x2 < 0) {
+                integrate(radii, K(i + 1, j), K(i, j), -x2, -x1, y, parts);
+                push(0, true, i, j);
+            } else {
+                integrate(radii, zx[j - ly], K(i, j), 0.0, -x1, y, parts);
+                push(0, true, i, j);
+                integrate(radii, zx[j - ly], K(i + 1, j), 0.0, x2, y, parts);
+                push(0, false, i, j);
+            }
+        }
+    }
+    for (int i = lx; i <= rx; i++) {
+        const double x = X(i);
+        for (int j = ly; j < ry; j++) {
+            const double y1 = Y(j), y2 = Y(j + 1);
+            if (y1 > 0 && y2 > 0) {
+                integrate(radii, K(i, j), K(i, j + 1), y1, y2, x, parts);
+                push(1, false, i, j);
+            } else if (y1 < 0 && y2 < 0) {
+                integrate(radii, K(i, j + 1), K(i, j), -y2, -y1, x, parts);
+                push(1, true, i, j);
+            } else {
+                integrate(radii, zy[i - lx], K(i, j), 0.0, -y1, x, parts);
+                push(1, true, i, j);
+                integrate(radii, zy[i - lx], K(i, j + 1), 0.0, y2, x, parts);
+                push(1, false, i, j);
+            }
+        }
+    }
+    const int ncell = 4 * nx * ny;
+    rowptr.assign(ncomp, {});
+    terms.assign(ncomp, {});
+    for (int c = 0; c < ncomp; c++) {
+        std::vector<int> &rp = rowptr[c];
+        rp.assign(ncell + 1, 0);
+        for (const Ev &e : evs) {
+            if ((e.dir == 0 ? kLvFacX[kind][c] : kLvFacY[kind][c]) == 0) continue;
+            for (int k = 0; k < e.ncell; k++) rp[e.cell[k] + 1] += e.np;
+        }
+        for (int r = 0; r < ncell; r++) rp[r + 1] += rp[r];
+        std::vector<int> fill(rp.begin(), rp.end() - 1);
+        std::vector<Term> &tl = terms[c];
+        tl.resize(rp[ncell]);
+        for (const Ev &e : evs) {
+            const int fac = e.dir == 0 ? kLvFacX[kind][c] : kLvFacY[kind][c];
+            if (fac == 0) continue;
+            const int src = e.dir == 0 ? kLvSrcX[kind][c] : kLvSrcY[kind][c];
+            const int q = e.dir == 0 ? (e.symm ? kLvQXS[kind][c] : kLvQX[kind][c])
+                                     : (e.symm ? kLvQYS[kind][c] : kLvQY[kind][c]);
+            for (int k = 0; k < e.ncell; k++) {
+                const double wgt = (double)(e.sign[k] * q);
+                for (int pi = 0; pi < e.np; pi++) {
+                    const SegF &p = all[e.p0 + pi];
+                    tl[fill[e.cell[k]]++] = Term{p.seg, src - 1, wgt * fac_a(p.f, fac), wgt * fac_b(p.f, fac)};
+                }
+            }
+        }
+    }
+}
+
+// ScalarPlansCreater.FindRhoMin(numberOfCells, cellSize, shift) for the
+// anomaly at the origin (ScalarPlansCreater.cs:240-262), in integer
+// micrometres as the reference's decimal arithmetic is exact.
+double level_rho_min_1d(int n, double cell, double shift) {
+    auto um = [](double v) { return std::llround(v * 1e6); };
+    const long long c = um(cell), sh = um(shift);
+    const long long a_start = -c / 2, a_end = c * n - c / 2;
+    const long long y_start = sh - c / 2, y_end = y_start + c * n;
+    auto between = [](long long v, long long lo, long long hi) { return v >= lo && v <= hi; };
+    if (between(y_start, a_start, a_end) || between(y_end, a_start, a_end)) {
+        const long long rem = std::llabs(a_start - y_start) % c;
+        if (rem == 0) return (double)(c / 2) * 1e-6;
+        return (double)std::llabs(c / 2 - rem) * 1e-6;
+    }
+    const long long lc = 0, rc = c * (n - 1);
+    const long long v = std::min(std::min(std::llabs(y_start - lc), std::llabs(y_start - rc)),
+                                 std::min(std::llabs(y_end - lc), std::llabs(y_end - rc)));
+    return (double)v * 1e-6;
+}
+
+// FindRhoMaxByFourPoints (ScalarPlansCreater.cs:220-233)
+double level_rho_max4(const GreenModel &m, double sx, double sy, double x0, double y0) {
+    const double x1 = sx - m.dx / 2, y1 = sy - m.dy / 2, x2 = x1 + m.dx * m.nx, y2 = y1 + m.dy * m.ny;
+    auto d = [](double a, double b) { return std::sqrt(a * a + b * b); };
+    return std::max(std::max(d(x1 - x0, y1 - y0), d(x2 - x0, y1 - y0)), std::max(d(x2 - x0, y2 - y0), d(x1 - x0, y2 - y0)));
+}
+
 }  // namespace
 
 // ModelUtils.FindCorrespondingBackgroundLayerIndex (ModelUtils.cs:27-50)
@@ -809,7 +1134,7 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
             ev = tm ? tm->begin(EGX_K_GREEN_HANKEL, s) : -1;
             k_hankel<<<(unsigned)((nh_threads + 127) / 128), 128, 0, s>>>(d_U.as<double2>(), nu, ntrans, nl_total,
                                                                            col0[it], nrho, drho, dg, dflags, dneg,
-                                                                           d_I.as<double2>(), nrad);
+                                                                           d_I.as<double2>(), nrad, 2.0 * M_PI);
             if (tm) tm->end(ev, s);
             // the per-item uploads above reuse buffers: finish before the next item
             EGX_CUDA(cudaStreamSynchronize(s));
@@ -903,6 +1228,188 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
         }
     }
     (void)t_start;
+}
+
+int level_components(int kind) { return kind == 0 ? 8 : 7; }
+
+void build_level_green(const GreenModel &m, int n_hankels, double z, double shx, double shy, int kind, cudaStream_t s,
+                       DevBuf &out, long *launches, GreenWorkspace &w) {
+    EGX_CHECK(m.nx > 0 && m.ny > 0 && m.nz > 0 && m.dx > 0 && m.dy > 0, EGX_ERR_INVALID, "bad model dimensions");
+    EGX_CHECK(kind == 0 || kind == 1, EGX_ERR_INVALID, "level tensor kind must be 0 (E) or 1 (H)");
+    const int L = (int)m.bg_thick.size();
+    EGX_CHECK(L >= 3 && L <= kMaxLayers, EGX_ERR_INVALID, "background must have 3.." + std::to_string(kMaxLayers) +
+                                                              " layers including both half-spaces");
+    static bool taps_loaded = false;
+    if (!taps_loaded) {
+        EGX_CUDA(cudaMemcpyToSymbol(c_h0, kHankelJ0, sizeof(kHankelJ0)));
+        EGX_CUDA(cudaMemcpyToSymbol(c_h1, kHankelJ1, sizeof(kHankelJ1)));
+        taps_loaded = true;
+    }
+    // ---- background (as build_green)
+    LayerArgs la{};
+    la.L = L;
+    la.omega = m.omega;
+    std::vector<double> tops(L + 1);
+    tops[0] = m.zero_air_level;
+    for (int k = 0; k < L; k++) tops[k + 1] = tops[k] + m.bg_thick[k];
+    std::vector<cd> zb(L);
+    for (int k = 0; k < L; k++) {
+        zb[k] = cd(m.bg_sigma[k], -m.omega * kEps0);
+        la.zeta[k] = make_double2(zb[k].real(), zb[k].imag());
+        la.thick[k] = m.bg_thick[k];
+        la.tops[k] = tops[k];
+    }
+    la.tops[L] = tops[L];
+    for (int k = 0; k < L - 1; k++) {
+        cd v = zb[k + 1] / zb[k];
+        la.alpha_s[k] = make_double2(v.real(), v.imag());
+    }
+    for (int k = 1; k < L; k++) {
+        cd v = zb[k - 1] / zb[k];
+        la.beta_s[k] = make_double2(v.real(), v.imag());
+    }
+    // ---- plan (CreateForAnomalyToObservationLevels, ScalarPlansCreater.cs:51-66)
+    const double step = rho_step();
+    double rho_min = std::min(level_rho_min_1d(m.nx, m.dx, shx), level_rho_min_1d(m.ny, m.dy, shy));
+    const double ex = m.dx * (m.nx - 1), ey = m.dy * (m.ny - 1);
+    const double rho_max = std::max(std::max(level_rho_max4(m, shx, shy, 0, 0), level_rho_max4(m, shx, shy, 0, ey)),
+                                    std::max(level_rho_max4(m, shx, shy, ex, ey), level_rho_max4(m, shx, shy, ex, 0)));
+    const bool add_zero = rho_min <= 0;
+    if (add_zero) rho_min = std::min(m.dx, m.dy) * 0.001;
+    const int nh = std::abs(n_hankels);
+    EGX_CHECK(nh >= 1, EGX_ERR_INVALID, "NumberOfHankels must be non-zero");
+    std::vector<std::vector<double>> items;
+    items.push_back(rho_from_min(rho_min, rho_max, step));
+    {
+        const double r2 = items[0].back(), r1 = items[0][items[0].size() - 2], lin = (r2 - r1) / nh;
+        for (int i = 1; i < nh; i++) items.push_back(rho_from_max(rho_min, r2 - i * lin, step));
+    }
+    struct RI {
+        double r;
+        int item, idx;
+    };
+    std::vector<RI> all;
+    if (add_zero) all.push_back({0.0, 0, -1});
+    for (int it = 0; it < (int)items.size(); it++)
+        for (int j = 0; j < (int)items[it].size(); j++) all.push_back({items[it][j], it, j});
+    std::stable_sort(all.begin(), all.end(), [](const RI &a, const RI &b) { return a.r < b.r; });
+    std::vector<double> radii(all.size());
+    std::vector<std::vector<int>> gidx(items.size());
+    for (size_t it = 0; it < items.size(); it++) gidx[it].resize(items[it].size());
+    for (size_t g = 0; g < all.size(); g++) {
+        radii[g] = all[g].r;
+        if (all[g].idx >= 0) gidx[all[g].item][all[g].idx] = (int)g;
+        if (g > 0) EGX_CHECK(radii[g] != radii[g - 1], EGX_ERR_INVALID, "duplicate radii across plan items");
+    }
+    const int nrad = (int)radii.size();
+    std::vector<std::vector<double>> lams;
+    std::vector<long> col0;
+    long nl_total = 0;
+    for (auto &rho : items) {
+        lams.push_back(lambdas_for(rho, step));
+        col0.push_back(nl_total);
+        nl_total += (long)lams.back().size();
+    }
+    // ---- transceivers: the level point above/below/inside each anomaly layer
+    std::vector<double> bthick(m.bg_thick.begin(), m.bg_thick.end());
+    std::vector<Trans> tl;
+    for (int k = 0; k < m.nz; k++) {
+        Trans t;
+        t.r1 = t.r2 = z;
+        t.s1 = m.depth[k];
+        t.s2 = m.depth[k] + m.thick[k];
+        t.r = layer_of(tops, bthick, z);
+        t.s = layer_of(tops, bthick, t.s1 + (t.s2 - t.s1) / 2);
+        EGX_CHECK(t.r + 1 < L && t.s + 1 < L, EGX_ERR_MODEL, "level or anomaly layer inside the lower half-space");
+        t.kase = (z > t.s1 && z < t.s2) ? 0 : (z >= t.s2 ? 1 : 2);
+        tl.push_back(t);
+    }
+    const int ntrans = m.nz;
+    const int nu = kind == 0 ? 5 : 4;
+    // Hankel order and signs (CalculateHankelForE/H, NormalizeAfterHankelForE/H)
+    const std::vector<int> use_h0 = kind == 0 ? std::vector<int>{0, 0, 1, 1, 0} : std::vector<int>{0, 0, 1, 1};
+    const std::vector<int> negate = kind == 0 ? std::vector<int>{1, 0, 0, 0, 0} : std::vector<int>{1, 1, 1, 0};
+    const double den = kind == 0 ? 2.0 * M_PI : 4.0 * M_PI;
+    Trans *dtrans = dev_upload(w.d_trans, tl, s);
+    int *dflags = dev_upload(w.d_flags, use_h0, s);
+    int *dneg = dev_upload(w.d_neg, negate, s);
+    double *radii_dev = dev_upload(w.d_radii, radii, s);
+    w.d_U.ensure((size_t)nu * ntrans * nl_total * sizeof(double2));
+    w.d_I.ensure((size_t)nu * ntrans * nrad * sizeof(double2));
+    for (size_t it = 0; it < items.size(); it++) {
+        const int nl = (int)lams[it].size();
+        double *dl = dev_upload(w.d_lam, lams[it], s);
+        w.d_lay.ensure((size_t)6 * L * nl * sizeof(double2));
+        k_layers<<<(nl + 127) / 128, 128, 0, s>>>(dl, nl, la, w.d_lay.as<double2>());
+        const long nthreads = (long)ntrans * nl;
+        k_kernels_vtp<<<(unsigned)((nthreads + 127) / 128), 128, 0, s>>>(
+            dl, nl, w.d_lay.as<double2>(), la, dtrans, ntrans, kind, w.d_U.as<double2>(), nl_total, col0[it]);
+        const int nrho = (int)items[it].size();
+        double *drho = dev_upload(w.d_rho, items[it], s);
+        int *dg = dev_upload(w.d_gidx, gidx[it], s);
+        const long nh_threads = (long)nu * ntrans * nrho;
+        k_hankel<<<(unsigned)((nh_threads + 127) / 128), 128, 0, s>>>(w.d_U.as<double2>(), nu, ntrans, nl_total,
+                                                                       col0[it], nrho, drho, dg, dflags, dneg,
+                                                                       w.d_I.as<double2>(), nrad, den);
+        EGX_CUDA(cudaStreamSynchronize(s));  // per-item uploads reuse buffers
+        if (launches) *launches += 3;
+    }
+    if (add_zero) {
+        const double a2 = step * step;
+        k_zero_rho<<<(nu * ntrans + 127) / 128, 128, 0, s>>>(w.d_I.as<double2>(), nu, ntrans, nrad, gidx[0][1],
+                                                             gidx[0][2], a2);
+        if (launches) *launches += 1;
+    }
+    const int nseg = nrad - 1;
+    w.d_IA.ensure((size_t)nu * nseg * ntrans * sizeof(double2));
+    w.d_IB.ensure((size_t)nu * nseg * ntrans * sizeof(double2));
+    {
+        const long n = (long)nu * nseg * ntrans;
+        k_segments<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w.d_I.as<double2>(), nu, ntrans, nrad, radii_dev,
+                                                               w.d_IA.as<double2>(), w.d_IB.as<double2>());
+        if (launches) *launches += 1;
+    }
+    EGX_CUDA(cudaGetLastError());
+    // ---- face integration (term lists cached per geometry, shift and radii)
+    const int ncomp = level_components(kind);
+    {
+        std::vector<double> key = {(double)m.nx, (double)m.ny, m.dx, m.dy, shx, shy};
+        key.insert(key.end(), radii.begin(), radii.end());
+        if (key != w.lkey[kind]) {
+            std::vector<std::vector<int>> rp;
+            std::vector<std::vector<Term>> tt;
+            level_terms(m, radii, shx, shy, kind, ncomp, rp, tt);
+            for (int c = 0; c < ncomp; c++) {
+                dev_upload(w.lrow[kind][c], rp[c], s);
+                dev_upload(w.lterm[kind][c], tt[c], s);
+            }
+            EGX_CUDA(cudaStreamSynchronize(s));
+            w.lkey[kind] = key;
+        }
+    }
+    const long ncell = 4L * m.nx * m.ny;
+    const size_t comp_elems = (size_t)ncell * m.nz;
+    out.ensure((size_t)ncomp * comp_elems * sizeof(double2));
+    const int n0 = 2 * m.nx, n1 = 2 * m.ny;
+    FftPlan p0 = make_fft_plan(n0), p1 = make_fft_plan(n1);
+    {
+        std::vector<double> t0 = twiddles(n0), t1 = twiddles(n1);
+        dev_upload(w.tw0, t0, s);
+        dev_upload(w.tw1, t1, s);
+    }
+    for (int c = 0; c < ncomp; c++) {
+        double2 *g = out.as<double2>() + (size_t)c * comp_elems;
+        const long n = ncell * m.nz;
+        k_cells_level<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w.lrow[kind][c].as<int>(),
+                                                                  w.lterm[kind][c].as<Term>(), w.d_IA.as<double2>(),
+                                                                  w.d_IB.as<double2>(), ntrans, nseg, (int)ncell, g);
+        EGX_CUDA(cudaGetLastError());
+        // PerformGreenTensorFft: the full 2-D transform of every layer column
+        fft_lines<double>(g, n0, (long)n1 * m.nz, m.nz, m.nz, n1, n1, p1, w.tw1.as<double2>(), -1, s, launches);
+        fft_lines<double>(g, n1, m.nz, (long)n1 * m.nz, m.nz, n0, n0, p0, w.tw0.as<double2>(), -1, s, launches);
+        if (launches) *launches += 1;
+    }
+    EGX_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace egx

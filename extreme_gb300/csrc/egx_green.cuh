@@ -36,7 +36,22 @@ struct GreenWorkspace {
     DevBuf rowptr[6], terms[6];
     long nterms[6] = {};
     bool cached[6] = {};
+    // observation-level tensors (E: kind 0, H: kind 1): term lists per component,
+    // keyed by the lateral mesh, the level's shift and the radii
+    std::vector<double> lkey[2];
+    DevBuf lrow[2][8], lterm[2][8];
 };
+
+// Components of a level tensor: E (kind 0) xx yy zz xy xz yz zx zy, H (kind 1)
+// xx yx xy xz yz zx zy.
+int level_components(int kind);
+
+// Build the spectral anomaly-to-observation-level tensor of one kind at depth
+// z with the level's lateral shift, in FP64 on the device
+// (AtoOLevelGreenTensorCalculator.cs:21-126, AtoOCalculator.cs:120-176):
+// out = [component][2nx][2ny][nz] complex128.
+void build_level_green(const GreenModel &m, int n_hankels, double z, double shift_x, double shift_y, int kind,
+                       cudaStream_t s, DevBuf &out, long *launches, GreenWorkspace &ws);
 
 // Build the spectral tensor into `quad` (device, complex128, layout of
 // GreenDims: quadrant points x [xx|xy|yy|zz|xz|yz] blocks).

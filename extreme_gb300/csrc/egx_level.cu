@@ -1,0 +1,192 @@
+// Fields at an observation level and the MT responses.
+//
+// egx_level_fields builds the anomaly-to-observation-level tensors of E and H
+// in FP64 on the device (build_level_green, egx_green.cu;
+// AtoOLevelGreenTensorCalculator.cs:21-126) and convolves them with jQ
+// (ToOCalculator.CalculateAnomalyField, ToOCalculator.cs:21-125):
+//   k_level_pad + 2-D DFT   jQ into the zero-padded [2nx][2ny][3nz] buffer
+//                           (PrepareForForwardFft, Plan3Nz forward);
+//   k_level_contract        per spectral point the sum over the anomaly layers
+//                           (ZgemvAtoO, Native/Native.Matrix/full_zgemv.c:22-26)
+//                           in the component pattern of ApplyGreenTensorAlongZForE/H;
+//   inverse 2-D DFT + k_level_extract   3 columns, scaled by 1/(4 nx ny),
+//                           rows i < nx, j < ny (Plan3 backward, Zscal, ExtractData).
+// egx_mt_responses is host arithmetic on the two polarisations' total fields
+// (ResponseFunctionsCalculator.cs:36-51, PlainTextExporter.cs:322-420).
+#include <cmath>
+#include <complex>
+
+#include "egx_ctx.cuh"
+
+using namespace egx;
+
+namespace {
+
+__global__ void k_level_pad(const double2 *__restrict__ jq, int nx, int ny, int per, double2 *__restrict__ buf) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)nx * ny * per) return;
+    const long cell = idx / per;
+    const int b = (int)(idx - cell * per);
+    const int i = (int)(cell / ny), j = (int)(cell - (long)i * ny);
+    buf[((long)i * 2 * ny + j) * per + b] = jq[idx];
+}
+
+__device__ __forceinline__ void acc_mul(double2 &a, double2 g, double2 s, double sign) {
+    a.x += sign * (g.x * s.x - g.y * s.y);
+    a.y += sign * (g.x * s.y + g.y * s.x);
+}
+
+// one warp per spectral point p: out[p][3] from X[p][3nz] and G[c][p][nz]
+// (E components xx yy zz xy xz yz zx zy, H components xx yx xy xz yz zx zy)
+__global__ void k_level_contract(const double2 *__restrict__ X, const double2 *__restrict__ G, long P, int nz,
+                                 int kind, double2 *__restrict__ out) {
+    const long p = (long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (p >= P) return;
+    const double2 *x = X + p * 3 * nz;
+    const size_t cs = (size_t)P * nz;
+    const double2 *g = G + p * nz;
+    double2 ax = make_double2(0, 0), ay = ax, az = ax;
+    for (int k = lane; k < nz; k += 32) {
+        const double2 sx = x[k], sy = x[nz + k], sz = x[2 * nz + k];
+        auto gc = [&](int c) { return g[c * cs + k]; };
+        if (kind == 0) {
+            acc_mul(ax, gc(0), sx, 1);
+            acc_mul(ax, gc(3), sy, 1);
+            acc_mul(ax, gc(4), sz, 1);
+            acc_mul(ay, gc(3), sx, 1);
+            acc_mul(ay, gc(1), sy, 1);
+            acc_mul(ay, gc(5), sz, 1);
+            acc_mul(az, gc(6), sx, 1);
+            acc_mul(az, gc(7), sy, 1);
+            acc_mul(az, gc(2), sz, 1);
+        } else {
+            acc_mul(ax, gc(0), sx, -1);
+            acc_mul(ax, gc(2), sy, -1);
+            acc_mul(ax, gc(3), sz, -1);
+            acc_mul(ay, gc(1), sx, 1);
+            acc_mul(ay, gc(0), sy, 1);
+            acc_mul(ay, gc(4), sz, 1);
+            acc_mul(az, gc(5), sx, -1);
+            acc_mul(az, gc(6), sy, 1);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ax.x += __shfl_xor_sync(0xffffffffu, ax.x, o);
+        ax.y += __shfl_xor_sync(0xffffffffu, ax.y, o);
+        ay.x += __shfl_xor_sync(0xffffffffu, ay.x, o);
+        ay.y += __shfl_xor_sync(0xffffffffu, ay.y, o);
+        az.x += __shfl_xor_sync(0xffffffffu, az.x, o);
+        az.y += __shfl_xor_sync(0xffffffffu, az.y, o);
+    }
+    if (lane == 0) {
+        out[p * 3] = ax;
+        out[p * 3 + 1] = ay;
+        out[p * 3 + 2] = az;
+    }
+}
+
+__global__ void k_level_extract(const double2 *__restrict__ out3, int nx, int ny, double scale,
+                                double2 *__restrict__ field) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)nx * ny * 3) return;
+    const long cell = idx / 3;
+    const int c = (int)(idx - cell * 3);
+    const int i = (int)(cell / ny), j = (int)(cell - (long)i * ny);
+    const double2 v = out3[((long)i * 2 * ny + j) * 3 + c];
+    field[idx] = make_double2(scale * v.x, scale * v.y);
+}
+
+}  // namespace
+
+extern "C" {
+
+int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_hankels, double z, double shift_x,
+                     double shift_y, const double *jq, int nsrc, double *e, double *h, int where) {
+    if (!ctx) return EGX_ERR_INVALID;
+    try {
+        EGX_CHECK(model && jq && e && h && nsrc >= 1, EGX_ERR_INVALID, "bad level-field arguments");
+        EGX_CHECK(model->layer_depth && model->layer_thickness && model->bg_thickness && model->bg_sigma,
+                  EGX_ERR_INVALID, "null model arrays");
+        EGX_CHECK(omega > 0, EGX_ERR_INVALID, "omega must be positive");
+        set_device(ctx);
+        const GreenModel gm = green_model(model, omega);
+        const int nx = gm.nx, ny = gm.ny, nz = gm.nz, n0 = 2 * nx, n1 = 2 * ny, per = 3 * nz;
+        cudaStream_t s = ctx->stream;
+        ensure_twiddles(ctx, n0, n1);
+        build_level_green(gm, n_hankels, z, shift_x, shift_y, 0, s, ctx->lvl_g[0], &ctx->launches, ctx->gws);
+        build_level_green(gm, n_hankels, z, shift_x, shift_y, 1, s, ctx->lvl_g[1], &ctx->launches, ctx->gws);
+        const long N = (long)nx * ny * per, P = (long)n0 * n1, F = (long)nx * ny * 3;
+        ctx->lvl_x.ensure((size_t)P * per * sizeof(double2));
+        ctx->lvl_out.ensure((size_t)P * 3 * sizeof(double2));
+        if (where != EGX_DEVICE) {
+            ctx->lvl_in.ensure((size_t)N * sizeof(double2));
+            ctx->lvl_field.ensure((size_t)F * sizeof(double2));
+        }
+        double2 *X = ctx->lvl_x.as<double2>(), *O = ctx->lvl_out.as<double2>();
+        const double2 *tw0 = ctx->tw0_64.as<double2>(), *tw1 = ctx->tw1_64.as<double2>();
+        for (int i = 0; i < nsrc; i++) {
+            const double2 *src;
+            if (where == EGX_DEVICE) {
+                src = reinterpret_cast<const double2 *>(jq) + (size_t)i * N;
+            } else {
+                EGX_CUDA(cudaMemcpyAsync(ctx->lvl_in.p, jq + 2 * (size_t)i * N, N * sizeof(double2),
+                                         cudaMemcpyHostToDevice, s));
+                src = ctx->lvl_in.as<double2>();
+            }
+            k_level_pad<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(src, nx, ny, per, X);
+            EGX_CUDA(cudaGetLastError());
+            // forward DFT: y over the nx data rows (ny loaded), then x over all columns (nx loaded)
+            fft_lines<double>(X, nx, (long)n1 * per, per, per, ny, n1, ctx->p1, tw1, -1, s, &ctx->launches);
+            fft_lines<double>(X, n1, per, (long)n1 * per, per, nx, n0, ctx->p0, tw0, -1, s, &ctx->launches);
+            for (int kind = 0; kind < 2; kind++) {
+                k_level_contract<<<(unsigned)((P + 7) / 8), 256, 0, s>>>(X, ctx->lvl_g[kind].as<double2>(), P, nz,
+                                                                         kind, O);
+                EGX_CUDA(cudaGetLastError());
+                // inverse DFT of the 3 columns: x keeping rows < nx, then y keeping j < ny
+                fft_lines<double>(O, n1, 3, (long)n1 * 3, 3, n0, nx, ctx->p0, tw0, +1, s, &ctx->launches);
+                fft_lines<double>(O, nx, (long)n1 * 3, 3, 3, n1, ny, ctx->p1, tw1, +1, s, &ctx->launches);
+                double *dst_host = (kind == 0 ? e : h) + 2 * (size_t)i * F;
+                double2 *dst = where == EGX_DEVICE ? reinterpret_cast<double2 *>(dst_host) : ctx->lvl_field.as<double2>();
+                k_level_extract<<<(unsigned)((F + 255) / 256), 256, 0, s>>>(O, nx, ny, 1.0 / (4.0 * nx * ny), dst);
+                EGX_CUDA(cudaGetLastError());
+                if (where != EGX_DEVICE)
+                    EGX_CUDA(cudaMemcpyAsync(dst_host, dst, F * sizeof(double2), cudaMemcpyDeviceToHost, s));
+                ctx->launches += 2;
+            }
+            ctx->launches += 1;
+            EGX_CUDA(cudaStreamSynchronize(s));
+        }
+        check_device_error(ctx);
+    } catch (const egx::Error &err) {
+        return fail(ctx, err.code, err.what());
+    } catch (const std::exception &err) {
+        return fail(ctx, EGX_ERR_INVALID, err.what());
+    }
+    return EGX_OK;
+}
+
+int egx_mt_responses(const double *e1, const double *e2, const double *h1, const double *h2, long n, double omega,
+                     double *z, double *rho, double *phase) {
+    if (!e1 || !e2 || !h1 || !h2 || !z || !rho || !phase || n < 1 || !(omega > 0)) return EGX_ERR_INVALID;
+    typedef std::complex<double> cd;
+    const double mu0 = 4.0 * M_PI * 1.0e-7;
+    auto at = [](const double *v, long k, int c) { return cd(v[2 * (3 * k + c)], v[2 * (3 * k + c) + 1]); };
+    for (long k = 0; k < n; k++) {
+        const cd f11x = at(e1, k, 0), f11y = at(e1, k, 1), f12x = at(e2, k, 0), f12y = at(e2, k, 1);
+        const cd f21x = at(h1, k, 0), f21y = at(h1, k, 1), f22x = at(h2, k, 0), f22y = at(h2, k, 1);
+        const cd det = f21x * f22y - f22x * f21y;
+        const cd hi11 = f22y / det, hi12 = -f22x / det, hi21 = -f21y / det, hi22 = f21x / det;
+        const cd zz[4] = {f11x * hi11 + f12x * hi21, f11x * hi12 + f12x * hi22, f11y * hi11 + f12y * hi21,
+                          f11y * hi12 + f12y * hi22};
+        for (int c = 0; c < 4; c++) {
+            z[2 * (4 * k + c)] = zz[c].real();
+            z[2 * (4 * k + c) + 1] = zz[c].imag();
+            rho[4 * k + c] = std::norm(zz[c]) / (omega * mu0);
+            phase[4 * k + c] = std::arg(zz[c]) * (180.0 / M_PI);
+        }
+    }
+    return EGX_OK;
+}
+
+}  // extern "C"

@@ -26,6 +26,7 @@ EXPORTS = [
     "egx_op_prepare", "egx_op_apply", "egx_op_apply_c64", "egx_fft2d",
     "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products", "egx_dot_products_static",
     "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_read",
+    "egx_level_fields", "egx_mt_responses",
 ]
 
 # kernel kinds of egx_profile_read
@@ -111,6 +112,8 @@ def load(path=None):
     lib.egx_plane_wave.argtypes = [C.POINTER(Model), d, d, vp, vp]
     lib.egx_solve_sources.argtypes = [vp, vp, vp, vp, vp, vp, vp, i, C.POINTER(SourceParams), vp, vp,
                                       C.POINTER(Result), i]
+    lib.egx_level_fields.argtypes = [vp, C.POINTER(Model), d, i, d, d, d, vp, i, vp, vp, i]
+    lib.egx_mt_responses.argtypes = [vp, vp, vp, vp, C.c_long, d, vp, vp, vp]
     lib.egx_profile.argtypes = [vp, i]
     lib.egx_profile_read.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_double)]
     _lib = lib
@@ -306,6 +309,18 @@ class Context:
             self._check(rc)
         return jq, chi, [r.as_dict() for r in res]
 
+    def level_fields(self, model, omega, jq, z=0.0, shift_x=0.0, shift_y=0.0, n_hankels=10):
+        """Anomalous E and H at the observation level z for jq [nsrc, N]
+        (host arrays): returns (e, h), each [nsrc, nx, ny, 3] complex128."""
+        jq = _c128(jq).reshape(-1, model.nx * model.ny * 3 * model.nz)
+        nsrc = jq.shape[0]
+        e = np.empty((nsrc, model.nx, model.ny, 3), np.complex128)
+        h = np.empty_like(e)
+        ms = model_struct(model)
+        self._check(self.lib.egx_level_fields(self.h, C.byref(ms.s), omega, n_hankels, z, shift_x, shift_y,
+                                              _ptr(jq), nsrc, _ptr(e), _ptr(h), HOST))
+        return e, h
+
     def profile(self, enable=True):
         self._check(self.lib.egx_profile(self.h, int(enable)))
 
@@ -399,3 +414,19 @@ def model_struct(model):
                  ms.depth.ctypes.data_as(dp), ms.thick.ctypes.data_as(dp), len(ms.bg_t),
                  float(model.section.zero_air_level), ms.bg_t.ctypes.data_as(dp), ms.bg_s.ctypes.data_as(dp))
     return ms
+
+
+def mt_responses(e1, e2, h1, h2, omega):
+    """Impedance [n, 2, 2], apparent resistivity [n, 2, 2] (Ohm m) and phase
+    [n, 2, 2] (degrees) from the total fields [n, 3] of polarisation X (e1, h1)
+    and Y (e2, h2) (egx_mt_responses)."""
+    lib = load()
+    arrs = [_c128(a).reshape(-1, 3) for a in (e1, e2, h1, h2)]
+    n = arrs[0].shape[0]
+    z = np.empty((n, 2, 2), np.complex128)
+    rho = np.empty((n, 2, 2))
+    ph = np.empty((n, 2, 2))
+    rc = lib.egx_mt_responses(*[_ptr(a) for a in arrs], n, omega, _ptr(z), _ptr(rho), _ptr(ph))
+    if rc != OK:
+        raise EgxError(rc, "egx_mt_responses: bad arguments")
+    return z, rho, ph

@@ -201,6 +201,23 @@ int egx_solve_sources(egx_ctx *ctx, egx_green *g, const double *zeta, const doub
                       const double *e0, const int *pol, int nsrc, const egx_source_params *p, double *chi,
                       double *jq, egx_result *res, int where);
 
+/* ---- fields at an observation level and MT responses --------------------- */
+/* Anomalous E and H at the observation level z (with its lateral shift) of
+ * nsrc current distributions jq [nsrc][N] (AtoOCalculator.CalculateAnomalyFieldE/H,
+ * AtoOCalculator.cs:68-176; ToOCalculator.CalculateAnomalyField,
+ * ToOCalculator.cs:21-125). The level tensors of E and H are built in FP64 on
+ * the device (AtoOLevelGreenTensorCalculator.cs:21-126). e, h: [nsrc][nx][ny][3]
+ * complex, anomalous part only (the normal field is egx_plane_wave at z). */
+int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_hankels, double z, double shift_x,
+                     double shift_y, const double *jq, int nsrc, double *e, double *h, int where);
+/* Impedance, apparent resistivity and phase at n sites from the total fields
+ * of polarisation X (e1, h1) and Y (e2, h2), each [n][3] complex, host arrays
+ * (ResponseFunctionsCalculator.CalculateTensor, ResponseFunctionsCalculator.cs:36-51;
+ * PlainTextExporter.cs:360-420): z [n][4] complex (xx, xy, yx, yy),
+ * rho [n][4] in Ohm m, phase [n][4] in degrees. */
+int egx_mt_responses(const double *e1, const double *e2, const double *h1, const double *h2, long n, double omega,
+                     double *z, double *rho, double *phase);
+
 /* ---- per-kernel device time ---------------------------------------------- */
 /* Instrumented kernels; add EGX_K_C64 for the complex64 variants. */
 enum {
