@@ -2,14 +2,17 @@
 
 One step is one MT solve at one frequency: the Green tensor built in FP64 on
 the device (stored complex64 for the inner solver and complex128 for the
-refinement residual), then both polarisations solved to a 1e-6 relative true
+refinement residual), both polarisations solved to a 1e-6 relative true
 residual by the mixed-precision solve (complex64 FGMRES with a GMRES
-preconditioner inside FP64 iterative refinement). Steps cycle over the
+preconditioner inside FP64 iterative refinement), then E and H at the
+surface (level tensors built in FP64) and the impedance, apparent
+resistivity and phase at all 256x256 cell centres. Steps cycle over the
 model's four frequencies (1e-3 .. 10 Hz, log-spaced).
 
 Keys of the JSON line beyond the common ones:
   e2e          the same solves through the C ABI with host buffers
-               (zeta, zeta0, dz, E0 copied in, jQ of both polarisations out);
+               (zeta, zeta0, dz, E0 copied in; surface E and H of both
+               polarisations out);
   roofline     the complex64 block-contraction kernel, its CUDA-event time on
                the library's stream during the timed region, against the
                measured HBM copy bandwidth;
@@ -181,20 +184,45 @@ def run_ours(args, rank, world, local):
     zeta0_d = [torch.from_numpy(z0.view(np.float64)).to(dev) for _, z0 in host_in]
     e0_d = [torch.from_numpy(e.reshape(-1).view(np.float64)).to(dev) for e in host_e0]
     jq_d = torch.empty(2 * n * 2, dtype=torch.float64, device=dev)
+    nf3 = m.nx * m.ny * 3
+    e_d = torch.empty(2 * nf3 * 2, dtype=torch.float64, device=dev)
+    h_d = torch.empty_like(e_d)
+    pw = [egx.plane_wave(m, freq_to_omega(f), 0.0) for f in freqs]
+
+    def responses(k, e, h):
+        """Total fields at the surface (anomalous + plane wave) and the MT
+        responses of all cell centres (Mt3DForwardSolver.cs:300-337)."""
+        e_n, h_n = pw[k]
+        e = e.reshape(2, nf3 // 3, 3).copy()
+        h = h.reshape(2, nf3 // 3, 3).copy()
+        e[0, :, 0] += e_n
+        h[0, :, 1] += h_n
+        e[1, :, 1] += e_n
+        h[1, :, 0] -= h_n
+        return egx.mt_responses(e[0], e[1], h[0], h[1], freq_to_omega(freqs[k]))
     torch.cuda.synchronize(dev)
 
     def step(i, where):
+        """One MT solve: Green tensor, both polarisations to jQ, fields at the
+        surface and the responses at every cell centre."""
         k = i % nf
-        g = ctx.green_build(m, freq_to_omega(freqs[k]), 10, egx.PREC_MIXED)
+        omega = freq_to_omega(freqs[k])
+        g = ctx.green_build(m, omega, 10, egx.PREC_MIXED)
         try:
             if where == egx.DEVICE:
-                return ctx.solve_sources(g, None, None, m.layer_thickness, None, [0, 1], precision=egx.PREC_MIXED,
-                                         mixed=mixed, where=egx.DEVICE,
-                                         dev_ptrs=dict(zeta=zeta_d[k].data_ptr(), zeta0=zeta0_d[k].data_ptr(),
-                                                       e0=e0_d[k].data_ptr(), jq=jq_d.data_ptr()))
-            z, z0 = host_in[k]
-            _, _, res = ctx.solve_sources(g, z, z0, m.layer_thickness, host_e0[k], [0, 1],
-                                          precision=egx.PREC_MIXED, mixed=mixed)
+                res = ctx.solve_sources(g, None, None, m.layer_thickness, None, [0, 1], precision=egx.PREC_MIXED,
+                                        mixed=mixed, where=egx.DEVICE,
+                                        dev_ptrs=dict(zeta=zeta_d[k].data_ptr(), zeta0=zeta0_d[k].data_ptr(),
+                                                      e0=e0_d[k].data_ptr(), jq=jq_d.data_ptr()))
+                ctx.level_fields_dev(m, omega, jq_d.data_ptr(), 2, e_d.data_ptr(), h_d.data_ptr(), z=0.0)
+                e = e_d.cpu().numpy().view(np.complex128)
+                h = h_d.cpu().numpy().view(np.complex128)
+            else:
+                z, z0 = host_in[k]
+                jq, _, res = ctx.solve_sources(g, z, z0, m.layer_thickness, host_e0[k], [0, 1],
+                                               precision=egx.PREC_MIXED, mixed=mixed)
+                e, h = ctx.level_fields(m, omega, jq, z=0.0)
+            responses(k, e, h)
             return res
         finally:
             g.free()
@@ -247,7 +275,7 @@ def run_ours(args, rank, world, local):
     barrier()
     ms_e2e = max(e0_ev.elapsed_time(e1_ev), (time.perf_counter() - t1) * 1e3)
     h2d = m.nx * m.ny * m.nz * 16 + m.nz * 16 + m.nz * 8 + 2 * m.nz * 16
-    d2h = 2 * n * 16
+    d2h = 2 * 2 * nf3 * 16   # E and H of both polarisations at the surface
 
     # ---- plain FP64 (the reference algorithm) at frequency index 1
     plain = None
@@ -257,9 +285,12 @@ def run_ours(args, rank, world, local):
         p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         p0.record(stream)
         g = ctx.green_build(m, freq_to_omega(freqs[k]), 10, egx.PREC_FP64)
-        _, _, pres = ctx.solve_sources(g, z, z0, m.layer_thickness, host_e0[k], [0, 1], precision=egx.PREC_FP64,
-                                       fgmres=dict(m_out=15, m_in=10, tol=1e-6, max_restarts=100))
+        jq_p, _, pres = ctx.solve_sources(g, z, z0, m.layer_thickness, host_e0[k], [0, 1],
+                                          precision=egx.PREC_FP64,
+                                          fgmres=dict(m_out=15, m_in=10, tol=1e-6, max_restarts=100))
         g.free()
+        e_p, h_p = ctx.level_fields(m, freq_to_omega(freqs[k]), jq_p, z=0.0)
+        responses(k, e_p, h_p)
         p1.record(stream)
         torch.cuda.synchronize(dev)
         tplain = p0.elapsed_time(p1)
@@ -301,7 +332,8 @@ def run_ours(args, rank, world, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64 (inner) / c128 (outer)",
         "data": "synthetic: seeded random model (5-layer background, 20 boxes), no dataset",
-        "config": {"workload": "%s model %dx%dx%d, %d frequencies %.0e..%.0e Hz cycled, 2 polarisations per solve"
+        "config": {"workload": "%s model %dx%dx%d, %d frequencies %.0e..%.0e Hz cycled, 2 polarisations per solve, "
+                               "surface E/H and impedance/rho_a/phase at all cell centres"
                                % (args.workload, m.nx, m.ny, m.nz, nf, freqs[0], freqs[-1]),
                    "method": "mixed precision (complex64 FGMRES(30)+GMRES(10) inside FP64 refinement, tol 1e-6); "
                              "learned preconditioner not used",

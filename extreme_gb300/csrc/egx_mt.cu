@@ -219,9 +219,22 @@ int egx_solve_sources(egx_ctx *ctx, egx_green *g, const double *zeta, const doub
                                                              e0d + (size_t)i * nz, pol[i], nz, ncell, js + i * n);
         }
         ctx->launches += nsrc;
-        // chi0 = K_chi0 jS for all sources in one apply
+        // chi0 = K_chi0 jS for all sources in one apply; the mixed form applies
+        // it in complex64 (its error, ~1e-7, stays far below the 1e-6 target;
+        // the refinement's residual against this chi0 is still complex128)
         prepare_device(ctx, g, dz, EGX_OP_CHI0);
-        apply_dev<double>(ctx, js, chi0, nsrc);
+        if (p->precision == EGX_PREC_MIXED && ctx->prepared32) {
+            ctx->xin32.ensure((size_t)nsrc * n * sizeof(float2));
+            ctx->yout32.ensure((size_t)nsrc * n * sizeof(float2));
+            float2 *js32 = ctx->xin32.as<float2>(), *chi32 = ctx->yout32.as<float2>();
+            convert_d2f(js, js32, (long)nsrc * n, 1.0, s);
+            apply_dev<float>(ctx, js32, chi32, nsrc);
+            EGX_CUDA(cudaMemsetAsync(chi0, 0, (size_t)nsrc * n * sizeof(double2), s));
+            convert_f2d_add(chi32, chi0, (long)nsrc * n, 1.0, s);
+            ctx->launches += 2;
+        } else {
+            apply_dev<double>(ctx, js, chi0, nsrc);
+        }
         prepare_device(ctx, g, dz, EGX_OP_A);
         for (int i = 0; i < nsrc; i++) {
             double2 *x = xs + (size_t)i * n;

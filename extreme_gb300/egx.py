@@ -321,6 +321,14 @@ class Context:
                                               _ptr(jq), nsrc, _ptr(e), _ptr(h), HOST))
         return e, h
 
+    def level_fields_dev(self, model, omega, jq_ptr, nsrc, e_ptr, h_ptr, z=0.0, shift_x=0.0, shift_y=0.0,
+                         n_hankels=10):
+        """egx_level_fields on device pointers (jq [nsrc][N], e/h [nsrc][nx][ny][3])."""
+        ms = model_struct(model)
+        self._check(self.lib.egx_level_fields(self.h, C.byref(ms.s), omega, n_hankels, z, shift_x, shift_y,
+                                              C.c_void_p(jq_ptr), nsrc, C.c_void_p(e_ptr), C.c_void_p(h_ptr),
+                                              DEVICE))
+
     def profile(self, enable=True):
         self._check(self.lib.egx_profile(self.h, int(enable)))
 

@@ -6,7 +6,8 @@ path, backed by ``libegx.so``.
 * :class:`Mt3DForwardSolver` -- ``Extreme.Cartesian.Magnetotellurics/Solver/Mt3DForwardSolver.cs:78-129``:
   ``solve(model, frequency)`` computes the anomaly-to-anomaly Green tensor
   (``CalculateGreenTensor``) and then solves polarisation X and Y
-  (``SolveForOneSource``: normal field, ``jS``, ``chi0``, FGMRES, ``Es``, ``jQ``).
+  (``SolveForOneSource``: normal field, ``jS``, ``chi0``, FGMRES, ``Es``, ``jQ``),
+  then the fields and responses at the observation levels.
 
 Everything numeric runs in the CUDA library: the host only forms the
 per-layer plane-wave field (``egx_normal_field``, ``nz`` scalars) and the
@@ -47,6 +48,21 @@ class MtSolution:
     jq: np.ndarray                      # [2, N]: pol X, pol Y
     chi: Optional[np.ndarray]
     results: List[dict] = field(default_factory=list)
+    levels: List["LevelResult"] = field(default_factory=list)
+
+
+@dataclass
+class LevelResult:
+    """Fields and responses at the cell centres of one observation level
+    (``AllFieldsAtLevel`` / ``AllFieldsAtSite`` and ``ResponseFunctionsCalculator``)."""
+    z: float
+    shift_x: float
+    shift_y: float
+    e: np.ndarray          # [2 pols, nx, ny, 3] total E
+    h: np.ndarray          # [2 pols, nx, ny, 3] total H
+    impedance: np.ndarray  # [nx*ny, 2, 2]
+    rho: np.ndarray        # [nx*ny, 2, 2] apparent resistivity, Ohm m
+    phase: np.ndarray      # [nx*ny, 2, 2] degrees
 
 
 def model_zeta(model: CartesianModel, omega: float):
@@ -69,7 +85,28 @@ class Mt3DForwardSolver:
         omega = freq_to_omega(frequency)
         return self.ctx.green_build(model, omega, self.settings.number_of_hankels, self.precision)
 
-    def solve(self, model: CartesianModel, frequency: float, green=None, want_chi=False) -> MtSolution:
+    def fields_at_level(self, model: CartesianModel, frequency: float, jq, z=0.0, shift_x=0.0, shift_y=0.0):
+        """Total fields of both polarisations at the level and the MT
+        responses (``Mt3DForwardSolver`` observation path:
+        ``AtoOCalculator`` anomalous fields + plane-wave normal fields,
+        ``Mt3DForwardSolver.cs:300-337``)."""
+        omega = freq_to_omega(frequency)
+        ea, ha = self.ctx.level_fields(model, omega, jq, z=z, shift_x=shift_x, shift_y=shift_y,
+                                       n_hankels=self.settings.number_of_hankels)
+        e_n, h_n = egx.plane_wave(model, omega, z)
+        e = ea.copy()
+        h = ha.copy()
+        e[0, ..., 0] += e_n   # pol X: E = (E0, 0, 0), H = (0, H0, 0)
+        h[0, ..., 1] += h_n
+        e[1, ..., 1] += e_n   # pol Y: E = (0, E0, 0), H = (-H0, 0, 0)
+        h[1, ..., 0] -= h_n
+        imp, rho, ph = egx.mt_responses(e[0], e[1], h[0], h[1], omega)
+        return LevelResult(z, shift_x, shift_y, e, h, imp, rho, ph)
+
+    def solve(self, model: CartesianModel, frequency: float, green=None, want_chi=False,
+              levels=()) -> MtSolution:
+        """Both polarisations to jQ; then, for every level (a depth or a
+        (depth, shift_x, shift_y) tuple), fields and responses."""
         omega = freq_to_omega(frequency)
         own = green is None
         if own:
@@ -87,4 +124,8 @@ class Mt3DForwardSolver:
         finally:
             if own:
                 green.free()
-        return MtSolution(frequency, jq, chi, res)
+        sol = MtSolution(frequency, jq, chi, res)
+        for lv in levels:
+            z, sx, sy = (lv, 0.0, 0.0) if np.isscalar(lv) else lv
+            sol.levels.append(self.fields_at_level(model, frequency, jq, z, sx, sy))
+        return sol

@@ -71,3 +71,8 @@ def test_surface_responses_match_oracle(egx_ctx):
     for a, b in ((0, 1), (1, 0)):
         assert rel(rho[:, a, b], rho_w[:, a, b]) < 10 * 1e-8
         assert np.max(np.abs(ph[:, a, b] - ph_w[:, a, b])) < 10 * 1e-8 * 180
+    # the same through the solver's observation-level path
+    lv = solver.solve(m, f, levels=[0.0]).levels[0]
+    assert rel(lv.e[0], want["e0"]) < 10 * 1e-8 and rel(lv.h[1], want["h1"]) < 10 * 1e-8
+    for a, b in ((0, 1), (1, 0)):
+        assert rel(lv.rho[:, a, b], rho_w[:, a, b]) < 10 * 1e-8
