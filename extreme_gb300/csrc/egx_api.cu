@@ -90,8 +90,10 @@ void gather_quadrant(int nx, int ny, int nz, const double *const comps[6], std::
 
 template <typename T>
 GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in, double tol, int max_restarts,
-                       bool check_true, int precond_kind, int *n_applies) {
-    const long n = nvec(ctx);
+                       bool check_true, int precond_kind, int *n_applies, int nrhs = 1) {
+    // nrhs > 1: one stacked system of nrhs blocks [nrhs][nvec], each Krylov
+    // step one nrhs-vector operator apply
+    const long n = nvec(ctx) * nrhs;
     const bool dbl = sizeof(T) == sizeof(double);
     char keybuf[160];
     snprintf(keybuf, sizeof keybuf, "%ld/%d/%d/%d/%d/%d", n, m_out, m_in, max_restarts, (int)check_true,
@@ -121,8 +123,8 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
     (*outer)->set_tol(tol);
     if (*inner) (*inner)->set_tol(tol);
     int applies = 0;
-    auto apply = [ctx, &applies](const C<T> *in, C<T> *out) {
-        apply_dev<T>(ctx, in, out, 1);
+    auto apply = [ctx, &applies, nrhs](const C<T> *in, C<T> *out) {
+        apply_dev<T>(ctx, in, out, nrhs);
         applies++;
     };
     (*outer)->apply = apply;
@@ -280,85 +282,105 @@ GmresResult fgmres_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_gmr
 // complex64 FGMRES on A d = r/||r||, x += ||r|| d, until ||r||/||b|| < tol.
 // The inner relative tolerance of a refinement at true residual be is
 // max(inner_tol, min(0.5, kInnerSafety * tol / be)).
+//
+// nrhs > 1 solves the nrhs systems A x_i = b_i ([nrhs][nvec] blocks) as one
+// stacked block-diagonal system: each block's residual is scaled to unit norm
+// before the inner solve, the inner tolerance is divided by sqrt(nrhs) (a
+// stacked residual below itol * sqrt(nrhs) bounds every block's by the same),
+// every apply is one nrhs-vector apply, and the refinement stops when every
+// block's own complex128 residual is below tol. true_be[i] per block.
 static const double kInnerSafety = 0.3;
 GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixed_params &p, int *applies,
-                      int *refinements, double *true_be) {
+                      int *refinements, double *true_be, int nrhs) {
     EGX_CHECK(p.m_out >= 1 && p.m_in >= 1 && p.max_outer >= 1 && p.tol > 0 && p.inner_tol > 0 &&
-                  p.inner_restarts >= 1,
+                  p.inner_restarts >= 1 && nrhs >= 1,
               EGX_ERR_INVALID, "bad mixed-solve parameters");
     EGX_CHECK(ctx->g->has32 && ctx->prepared32, EGX_ERR_STATE,
               "mixed solve needs a Green tensor built or uploaded with EGX_PREC_MIXED");
-    const long n = nvec(ctx);
-    ctx->mix_r.ensure(n * sizeof(double2));
-    ctx->mix_t.ensure(n * sizeof(double2));
-    ctx->mix_r32.ensure(n * sizeof(float2));
-    ctx->mix_d32.ensure(n * sizeof(float2));
+    const long n = nvec(ctx), N = n * nrhs;
+    ctx->mix_r.ensure(N * sizeof(double2));
+    ctx->mix_t.ensure(N * sizeof(double2));
+    ctx->mix_r32.ensure(N * sizeof(float2));
+    ctx->mix_d32.ensure(N * sizeof(float2));
     ctx->nrm_part.ensure(2048 * sizeof(double));
     ctx->nrm_out.ensure(sizeof(double));
     double2 *r = ctx->mix_r.as<double2>(), *t = ctx->mix_t.as<double2>();
     float2 *r32 = ctx->mix_r32.as<float2>(), *d32 = ctx->mix_d32.as<float2>();
-    auto norm64 = [&](const double2 *v) {
-        VecOps<double>::norm2(v, n, ctx->nrm_out.as<double>(), ctx->nrm_part.as<double>(), 1024, ctx->stream);
+    auto norm64 = [&](const double2 *v, long len) {
+        VecOps<double>::norm2(v, len, ctx->nrm_out.as<double>(), ctx->nrm_part.as<double>(), 1024, ctx->stream);
         ctx->launches += 2;
         double h;
         EGX_CUDA(cudaMemcpyAsync(&h, ctx->nrm_out.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));
         return std::sqrt(h);
     };
+    std::vector<double> bn(nrhs), rn(nrhs), be(nrhs);
+    // max over the blocks with a nonzero right-hand side (a zero block has x = 0)
+    auto residuals = [&](const double2 *rv) {
+        double m = 0;
+        for (int i = 0; i < nrhs; i++) {
+            rn[i] = bn[i] > 0 ? norm64(rv + i * n, n) : 0.0;
+            be[i] = bn[i] > 0 ? rn[i] / bn[i] : 0.0;
+            m = std::max(m, be[i]);
+        }
+        return m;
+    };
     int applies64 = 0, applies32 = 0;
     GmresResult out;
-    double bn = norm64(b);
-    if (bn == 0) {
-        VecOps<double>::zero(x, n, ctx->stream);
+    bool any = false;
+    for (int i = 0; i < nrhs; i++) {
+        bn[i] = norm64(b + i * n, n);
+        if (bn[i] == 0) VecOps<double>::zero(x + i * n, n, ctx->stream);
+        any = any || bn[i] > 0;
+    }
+    if (!any) {
         out.converged = true;
         *applies = 0;
         *refinements = 0;
-        *true_be = 0;
+        for (int i = 0; i < nrhs; i++) true_be[i] = 0;
         return out;
     }
     // r = b - A x; a zero initial guess needs no complex128 apply
-    double rn;
-    if (norm64(x) == 0) {
-        EGX_CUDA(cudaMemcpyAsync(r, b, n * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
-        rn = bn;
+    double bemax;
+    if (norm64(x, N) == 0) {
+        EGX_CUDA(cudaMemcpyAsync(r, b, N * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
+        bemax = residuals(r);
     } else {
-        apply_dev<double>(ctx, x, t, 1);
+        apply_dev<double>(ctx, x, t, nrhs);
         applies64++;
-        VecOps<double>::sub(b, t, r, n, ctx->stream);
+        VecOps<double>::sub(b, t, r, N, ctx->stream);
         ctx->launches++;
-        rn = norm64(r);
+        bemax = residuals(r);
     }
-    double be = rn / bn;
     int k = 0;
-    bool conv = be < p.tol;
+    bool conv = bemax < p.tol;
     while (!conv && k < p.max_outer) {
-        convert_d2f(r, r32, n, 1.0 / rn, ctx->stream);
-        VecOps<float>::zero(d32, n, ctx->stream);
-        ctx->launches += 1;
+        for (int i = 0; i < nrhs; i++) convert_d2f(r + i * n, r32 + i * n, n, rn[i] > 0 ? 1.0 / rn[i] : 0.0, ctx->stream);
+        VecOps<float>::zero(d32, N, ctx->stream);
+        ctx->launches += 1 + nrhs;
         int a32 = 0;
         // ask the inner solve only for the reduction still needed (with a
         // safety factor), never for less than inner_tol
-        double itol = std::max(p.inner_tol, std::min(0.5, kInnerSafety * p.tol / be));
+        double itol = std::max(p.inner_tol, std::min(0.5, kInnerSafety * p.tol / bemax)) / std::sqrt((double)nrhs);
         GmresResult ir = run_fgmres<float>(ctx, r32, d32, p.m_out, p.m_in, itol, p.inner_restarts, false,
-                                           EGX_PRECOND_GMRES, &a32);
+                                           EGX_PRECOND_GMRES, &a32, nrhs);
         applies32 += a32;
         out.iterations += ir.iterations;
         out.arnoldi_be = ir.arnoldi_be;
-        convert_f2d_add(d32, x, n, rn, ctx->stream);
-        apply_dev<double>(ctx, x, t, 1);
+        for (int i = 0; i < nrhs; i++) convert_f2d_add(d32 + i * n, x + i * n, n, rn[i], ctx->stream);
+        apply_dev<double>(ctx, x, t, nrhs);
         applies64++;
-        VecOps<double>::sub(b, t, r, n, ctx->stream);
-        ctx->launches += 2;
-        rn = norm64(r);
-        be = rn / bn;
+        VecOps<double>::sub(b, t, r, N, ctx->stream);
+        ctx->launches += 1 + nrhs;
+        bemax = residuals(r);
         k++;
-        conv = be < p.tol;
+        conv = bemax < p.tol;
     }
     out.converged = conv;
-    out.true_be = be;
+    out.true_be = bemax;
     *applies = applies64 + applies32;
     *refinements = k;
-    *true_be = be;
+    for (int i = 0; i < nrhs; i++) true_be[i] = be[i];
     return out;
 }
 

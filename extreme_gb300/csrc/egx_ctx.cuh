@@ -72,7 +72,7 @@ void upload_model(egx_ctx *ctx, egx_green *g, const double *zeta, const double *
 template <typename T> void apply_dev(egx_ctx *ctx, const C<T> *x, C<T> *y, int nrhs);
 GmresResult fgmres_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_gmres_params &p, int *applies);
 GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixed_params &p, int *applies,
-                      int *refinements, double *true_be);
+                      int *refinements, double *true_be, int nrhs = 1);
 int fail(egx_ctx *ctx, int code, const std::string &msg);
 // egx_model -> the build's model at angular frequency omega
 GreenModel green_model(const egx_model *model, double omega);

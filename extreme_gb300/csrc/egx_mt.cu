@@ -9,6 +9,7 @@
 // jQ = Es (zeta - zeta0) + jS (Forward/ForwardSolver.cs:186-436).
 #include <cmath>
 #include <complex>
+#include <vector>
 
 #include "egx_ctx.cuh"
 
@@ -236,29 +237,49 @@ int egx_solve_sources(egx_ctx *ctx, egx_green *g, const double *zeta, const doub
             apply_dev<double>(ctx, js, chi0, nsrc);
         }
         prepare_device(ctx, g, dz, EGX_OP_A);
+        const bool stacked = p->precision == EGX_PREC_MIXED && p->mixed.batch && nsrc > 1;
+        if (stacked) {
+            // all sources as one stacked system from zero: every operator
+            // apply covers every source
+            EGX_CUDA(cudaMemsetAsync(xs, 0, (size_t)nsrc * n * sizeof(double2), s));
+            int applies = 0, refinements = 0;
+            std::vector<double> tbe(nsrc, -1.0);
+            GmresResult r = mixed_dev(ctx, chi0, xs, p->mixed, &applies, &refinements, tbe.data(), nsrc);
+            for (int i = 0; i < nsrc; i++) {
+                res[i].converged = tbe[i] < p->mixed.tol;
+                res[i].iterations = r.iterations;
+                res[i].arnoldi_be = r.arnoldi_be;
+                res[i].true_be = tbe[i];
+                res[i].n_applies = applies + 1;  // applies of the operator to this source, + chi0
+                res[i].n_refinements = refinements;
+            }
+            if (!r.converged) status = fail(ctx, EGX_ERR_NOT_CONVERGED, "source solve did not converge");
+        }
         for (int i = 0; i < nsrc; i++) {
             double2 *x = xs + (size_t)i * n;
-            int applies = 0, refinements = 0;
-            double tbe = -1;
-            GmresResult r;
-            if (p->precision == EGX_PREC_FP64) {
-                // the reference starts FGMRES from chi0 (ForwardSolver.cs:300-306)
-                EGX_CUDA(cudaMemcpyAsync(x, chi0 + i * n, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-                r = fgmres_dev(ctx, chi0 + i * n, x, p->fgmres, &applies);
-                tbe = r.true_be;
-            } else {
-                // the refinement starts from zero: its first residual is chi0
-                // itself, which saves a complex128 apply
-                EGX_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double2), s));
-                r = mixed_dev(ctx, chi0 + i * n, x, p->mixed, &applies, &refinements, &tbe);
+            if (!stacked) {
+                int applies = 0, refinements = 0;
+                double tbe = -1;
+                GmresResult r;
+                if (p->precision == EGX_PREC_FP64) {
+                    // the reference starts FGMRES from chi0 (ForwardSolver.cs:300-306)
+                    EGX_CUDA(cudaMemcpyAsync(x, chi0 + i * n, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+                    r = fgmres_dev(ctx, chi0 + i * n, x, p->fgmres, &applies);
+                    tbe = r.true_be;
+                } else {
+                    // the refinement starts from zero: its first residual is chi0
+                    // itself, which saves a complex128 apply
+                    EGX_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double2), s));
+                    r = mixed_dev(ctx, chi0 + i * n, x, p->mixed, &applies, &refinements, &tbe);
+                }
+                res[i].converged = r.converged;
+                res[i].iterations = r.iterations;
+                res[i].arnoldi_be = r.arnoldi_be;
+                res[i].true_be = tbe;
+                res[i].n_applies = applies + 1;  // + the chi0 apply
+                res[i].n_refinements = refinements;
+                if (!r.converged) status = fail(ctx, EGX_ERR_NOT_CONVERGED, "source solve did not converge");
             }
-            res[i].converged = r.converged;
-            res[i].iterations = r.iterations;
-            res[i].arnoldi_be = r.arnoldi_be;
-            res[i].true_be = tbe;
-            res[i].n_applies = applies + 1;  // + the chi0 apply
-            res[i].n_refinements = refinements;
-            if (!r.converged) status = fail(ctx, EGX_ERR_NOT_CONVERGED, "source solve did not converge");
             if (chi)
                 EGX_CUDA(cudaMemcpyAsync(chi + 2 * (size_t)i * n, x, n * sizeof(double2),
                                          where == EGX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));

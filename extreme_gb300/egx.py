@@ -59,7 +59,7 @@ class GmresParams(C.Structure):
 
 class MixedParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_outer", C.c_int), ("m_out", C.c_int), ("m_in", C.c_int),
-                ("inner_tol", C.c_double), ("inner_restarts", C.c_int)]
+                ("inner_tol", C.c_double), ("inner_restarts", C.c_int), ("batch", C.c_int)]
 
 
 class SourceParams(C.Structure):
@@ -239,7 +239,7 @@ class Context:
     def mixed_solve(self, b, x0, tol=1e-6, max_outer=10, m_out=30, m_in=10, inner_tol=5e-7, inner_restarts=20):
         b = _c128(b)
         x = _c128(x0).copy()
-        p = MixedParams(tol, max_outer, m_out, m_in, inner_tol, inner_restarts)
+        p = MixedParams(tol, max_outer, m_out, m_in, inner_tol, inner_restarts, 0)
         r = Result()
         rc = self.lib.egx_mixed_solve(self.h, _ptr(b), _ptr(x), C.byref(p), C.byref(r), HOST)
         if rc not in (OK, ERR_NOT_CONVERGED):
@@ -248,7 +248,7 @@ class Context:
 
     def mixed_solve_dev(self, b_ptr, x_ptr, tol=1e-6, max_outer=10, m_out=30, m_in=10, inner_tol=5e-7,
                         inner_restarts=20):
-        p = MixedParams(tol, max_outer, m_out, m_in, inner_tol, inner_restarts)
+        p = MixedParams(tol, max_outer, m_out, m_in, inner_tol, inner_restarts, 0)
         r = Result()
         rc = self.lib.egx_mixed_solve(self.h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(p), C.byref(r), DEVICE)
         if rc not in (OK, ERR_NOT_CONVERGED):
@@ -287,7 +287,8 @@ class Context:
                                      fg.get("max_restarts", 100), fg.get("precond", PRECOND_GMRES),
                                      int(fg.get("check_true", True))),
                          MixedParams(mx.get("tol", 1e-6), mx.get("max_outer", 10), mx.get("m_out", 30),
-                                     mx.get("m_in", 10), mx.get("inner_tol", 5e-7), mx.get("inner_restarts", 20)))
+                                     mx.get("m_in", 10), mx.get("inner_tol", 5e-7), mx.get("inner_restarts", 20),
+                                     int(mx.get("batch", True))))
         res = (Result * nsrc)()
         if where == DEVICE:
             d = dev_ptrs

@@ -40,6 +40,7 @@ class MixedSettings:
     m_in: int = 10
     inner_tol: float = 5e-7
     inner_restarts: int = 20
+    batch: bool = True        # both polarisations as one stacked system
 
 
 @dataclass

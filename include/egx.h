@@ -86,6 +86,11 @@ typedef struct {
                              a refinement at true residual be asks only for
                              max(inner_tol, min(0.5, 0.3 * tol / be)) */
     int inner_restarts;
+    int batch;            /* egx_solve_sources with several sources: 1 solves
+                             them as one stacked block-diagonal system (every
+                             operator apply covers all sources, each source
+                             still checked against tol on its own residual);
+                             0 solves them one after the other */
 } egx_mixed_params;
 
 /* ResultInfo (Extreme.Fgmres/ResultInfo.cs) plus counters. */

@@ -50,14 +50,41 @@ def test_forward_fp64_matches_oracle(egx_ctx, oracle_small):
         assert rel(sol.jq[i], outs[p].jq) < 10 * 1e-8
 
 
-def test_forward_mixed_matches_oracle(egx_ctx, oracle_small):
+@pytest.mark.parametrize("batch", [True, False])
+def test_forward_mixed_matches_oracle(egx_ctx, oracle_small, batch):
     m, om, outs = oracle_small
     solver = Mt3DForwardSolver(ForwardSettings(residual=1e-8), precision=egx.PREC_MIXED,
-                               mixed=MixedSettings(tol=1e-6, inner_tol=1e-4), ctx=egx_ctx)
+                               mixed=MixedSettings(tol=1e-6, inner_tol=1e-4, batch=batch), ctx=egx_ctx)
     sol = solver.solve(m, 0.1)
     for i, p in enumerate("xy"):
         assert sol.results[i]["converged"] and sol.results[i]["true_be"] < 1e-6
         assert rel(sol.jq[i], outs[p].jq) < 2e-5
+    if batch:   # one stacked solve: shared iteration count
+        assert sol.results[0]["iterations"] == sol.results[1]["iterations"]
+
+
+def test_stacked_sources_scaled_and_zero(egx_ctx, oracle_small):
+    """Stacked mixed solve of sources whose right-hand sides differ by 1e6 in
+    norm, plus a zero source: every source reaches the tolerance on its own
+    residual, the zero source gives jQ = 0, and the scaled source gives the
+    scaled currents (the CIE is linear in E0)."""
+    m, om, outs = oracle_small
+    from extreme_gb300.forward import model_zeta
+    zeta, zeta0 = model_zeta(m, om.omega)
+    e0 = egx.normal_field(m, om.omega)
+    g = egx_ctx.green_build(m, om.omega, 10, egx.PREC_MIXED)
+    try:
+        e0s = np.stack([e0, 1e6 * e0, np.zeros_like(e0)])
+        jq, _, res = egx_ctx.solve_sources(g, zeta, zeta0, m.layer_thickness, e0s, [0, 1, 0],
+                                           precision=egx.PREC_MIXED,
+                                           mixed=dict(tol=1e-6, inner_tol=1e-4, batch=True))
+    finally:
+        g.free()
+    for r in res:
+        assert r["converged"] and r["true_be"] < 1e-6
+    assert rel(jq[0], outs["x"].jq) < 2e-5
+    assert rel(jq[1] / 1e6, outs["y"].jq) < 2e-5
+    assert not np.any(jq[2])
 
 
 def test_profile_counts_kernels(egx_ctx, oracle_small):
