@@ -43,10 +43,11 @@ sys.path.insert(0, ROOT)
 METRIC = "MT solves/s to 1e-6 residual (256x256x48): mixed+learned vs plain FP64, 1 GB300"
 
 # DRAM bytes (read + write) of one launch of the complex64 contraction at
-# 256x256x48: 1.4262 GB measured by ncu at 128x128x48 (16,641 stored points),
-# scaled by the algorithmic bytes (5.6765 GB / 1.4290 GB), which grow with the
-# stored points.
-CONTRACT_TRAFFIC_BYTES = 5.665e9
+# 256x256x48, by right-hand sides per launch, measured by ncu at 128x128x48
+# (16,641 stored points) and scaled by the algorithmic bytes, which grow with
+# the stored points. One: 1.4262 GB x 5.6765 / 1.4290; two (k_contract_sb3):
+# 1.5719 GB x 6.2805 / 1.5800.
+CONTRACT_TRAFFIC_BYTES = {1: 5.665e9, 2: 6.248e9}
 
 # Operator applications per polarisation of the reference algorithm
 # (complex128 FGMRES(15) with GMRES(10), tolerance 1e-6) on the 256x256x48
@@ -314,16 +315,20 @@ def run_ours(args, rank, world, local):
 
     # roofline of the contraction: algorithmic bytes per launch / event time.
     # Bytes = the stored complex64 Green blocks of the (nx+1)(ny+1) quadrant
-    # read once + the spectral buffer [2nx, 2ny, 3nz] complex64 read and written.
+    # read once + the spectral buffer [2nx, 2ny, 3nz] complex64 of every
+    # right-hand side of the launch read and written (two with the stacked solve).
     q = (m.nx + 1) * (m.ny + 1)
-    alg_bytes = q * c64_block_entries(m.nz) * 8 + 2 * (4 * m.nx * m.ny * 3 * m.nz * 8)
+    rhs = 2 if mixed["batch"] else 1
+    alg_bytes = q * c64_block_entries(m.nz) * 8 + rhs * 2 * (4 * m.nx * m.ny * 3 * m.nz * 8)
     peak, peak_src = load_peaks()
     achieved = alg_bytes / (kms / kc / 1e3) / 1e9 if kc else None
-    roofline = {"kernel": "k_contract_sb" if m.nz in (16, 32, 48) else "k_contract_mma", "bound": "hbm",
+    kname = ("k_contract_sb3" if rhs == 2 else "k_contract_sb") if m.nz in (16, 32, 48) else "k_contract_mma"
+    roofline = {"kernel": kname, "bound": "hbm", "rhs_per_launch": rhs,
                 "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4) if achieved else None, "peak_source": peak_src,
                 "algorithmic_bytes": alg_bytes, "ms_per_launch": round(kms / kc, 4) if kc else None,
-                "traffic": int(CONTRACT_TRAFFIC_BYTES) if (m.nx, m.ny, m.nz) == (256, 256, 48) else None}
+                "traffic": (int(CONTRACT_TRAFFIC_BYTES[rhs]) if CONTRACT_TRAFFIC_BYTES[rhs] and (m.nx, m.ny, m.nz) == (256, 256, 48)
+                            else None)}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

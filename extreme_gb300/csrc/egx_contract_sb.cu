@@ -430,6 +430,267 @@ __global__ void __launch_bounds__(Sb<NZ, NRHS>::THREADS, 1)
     }
 }
 
+// Two right-hand sides with three real products per complex product
+// (Gauss): T1 = Gr Xr, T2 = Gi Xi, T3 = (Gr + Gi)(Xr + Xi), Yr = T1 - T2,
+// Yi = T3 - T1 - T2. The eight columns of one n8 tile are the four points
+// sharing the stored block times the two right-hand sides (column 4 rhs + v),
+// so a (row tile, column tile) pair takes 3 products x 3 TF32 passes = 9 MMAs
+// where the embedded form takes 12. Each warp combines its partial sums to
+// (Yr, Yi) before the cross-warp reduction; when the partials do not fit
+// beside the other regions they reuse the stage's block buffer (free once
+// every warp is done with it) and the stage is refilled after the reduction.
+template <int NZ>
+struct Sb3 {
+    static constexpr int R = 3 * NZ, MT = R / 16, KT = R / 8, NB = NZ / 4;
+    static constexpr int SYM = NB * (NB + 1) / 2 * 16, ASY = NB * NB * 16, BS = 4 * SYM + 2 * ASY;
+    static constexpr int MG = 3, KG = 4, MPW = MT / MG, KMAX = (KT + KG - 1) / KG;
+    static constexpr int THREADS = 32 * MG * KG;
+    static constexpr int XB = 2 * R;  // complex per spectral point (two right-hand sides)
+    static constexpr uint32_t G_BYTES = BS * 8u;
+    static constexpr uint32_t X_BYTES = 4u * XB * 8u;
+    static constexpr uint32_t BF_BYTES = KT * 3u * 32u * 16u;
+    static constexpr uint32_t PART_BYTES = KG * MT * 2u * 4u * 32u * 4u;
+    static constexpr bool PART_IN_G = 2 * G_BYTES + 2 * X_BYTES + BF_BYTES + PART_BYTES > 227u * 1024u;
+    static constexpr uint32_t OFF_X = 2 * G_BYTES, OFF_BF = OFF_X + 2 * X_BYTES;
+    static constexpr uint32_t SMEM = PART_IN_G ? OFF_BF + BF_BYTES : OFF_BF + BF_BYTES + PART_BYTES;
+    static_assert(MT % MG == 0, "row tiles must split over the row groups");
+    static_assert(!PART_IN_G || PART_BYTES <= G_BYTES, "partials must fit in one block buffer");
+    static_assert(MT <= MG * KG, "one warp per row tile in the epilogue");
+    static_assert(G_BYTES % 128 == 0 && X_BYTES % 128 == 0, "stage alignment");
+    __host__ __device__ static constexpr int kt0(int kg) { return kg * KT / KG; }
+};
+
+template <int NZ>
+__global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
+    k_contract_sb3(float2 *buf, const float2 *__restrict__ G, const int nx, const int ny, const int B, const int rhs0,
+                   int *err) {
+    using P = Sb3<NZ>;
+    constexpr int R = P::R, MPW = P::MPW, KMAX = P::KMAX;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int status;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int mg = warp % P::MG, kg = warp / P::MG;
+    const int ktb = P::kt0(kg), kcnt = P::kt0(kg + 1) - ktb;
+    const uint32_t sG = saddr(smem), sX = sG + P::OFF_X, sBF = sG + P::OFF_BF;
+    const uint32_t bar0 = saddr(&bars[0]);
+    const long Q = (long)(nx + 1) * (ny + 1);
+    const int n1 = 2 * ny;
+
+    // A-fragment offsets in registers, built through the stage-0 block buffer
+    constexpr int TABN = MPW * KMAX * 2;
+    static_assert(P::MG * P::KG * TABN * 32 * 4 <= P::G_BYTES, "offset scratch must fit in one stage");
+    uint32_t tab[TABN];
+    {
+        uint32_t *scratch = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * TABN * 32 + lane;
+#pragma unroll 1
+        for (int p = 0; p < MPW * KMAX; p++) {
+            const int im = p / KMAX, ik = p - im * KMAX;
+            uint32_t w0 = 0, w1 = 0;
+            if (ik < kcnt) {
+                const int r0 = 16 * (mg * MPW + im) + g, c0 = 8 * (ktb + ik) + t;
+                w0 = (uint32_t)sb_index(NZ, r0, c0) | ((uint32_t)sb_index(NZ, r0 + 8, c0) << 16);
+                w1 = (uint32_t)sb_index(NZ, r0, c0 + 4) | ((uint32_t)sb_index(NZ, r0 + 8, c0 + 4) << 16);
+            }
+            scratch[(2 * p) * 32] = w0;
+            scratch[(2 * p + 1) * 32] = w1;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < TABN; j++) tab[j] = scratch[j * 32];
+    }
+
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        status = 0;
+    }
+    __syncthreads();
+
+    auto issue = [&](long qq, int stage) {
+        const int a = (int)(qq / (ny + 1)), bq = (int)(qq - (long)a * (ny + 1));
+        const int nkx = (a == 0 || a == nx) ? 1 : 2;
+        const int nky = (bq == 0 || bq == ny) ? 1 : 2;
+        const uint32_t bar = bar0 + 8 * stage;
+        bar_expect(bar, P::G_BYTES + (uint32_t)(nkx * nky) * (P::XB * 8u));
+        bulk_g2s(sG + stage * P::G_BYTES, G + qq * P::BS, P::G_BYTES, bar);
+        for (int p = 0; p < 4; p++) {
+            const int mx = p >> 1, my = p & 1;
+            if (mx < nkx && my < nky) {
+                const long pt = (long)(mx ? 2 * nx - a : a) * n1 + (my ? 2 * ny - bq : bq);
+                bulk_g2s(sX + stage * P::X_BYTES + p * (P::XB * 8u), buf + pt * B + (long)rhs0 * R, P::XB * 8u, bar);
+            }
+        }
+    };
+    long q = blockIdx.x;
+    if (tid == 0) {
+        if (q < Q) issue(q, 0);
+        if (q + gridDim.x < Q) issue(q + gridDim.x, 1);
+    }
+
+    for (int it = 0; q < Q; q += gridDim.x, it++) {
+        const int stage = it & 1;
+        const uint32_t parity = (it >> 1) & 1;
+        const uint32_t bar = bar0 + 8 * stage;
+        if (tid == 0 && !bar_wait(bar, parity, kWait)) status = 1;
+        __syncthreads();
+        if (status) {
+            if (tid == 0) {
+                atomicExch(err, EGX_ERR_TIMEOUT);
+                bar_wait(bar0 + 8 * (stage ^ 1), ((it + 1) >> 1) & 1, kWait);
+            }
+            return;
+        }
+        bar_wait(bar, parity, kWait);  // acquire the stage for every thread
+        const int a = (int)(q / (ny + 1)), bq = (int)(q - (long)a * (ny + 1));
+        const int nkx = (a == 0 || a == nx) ? 1 : 2;
+        const int nky = (bq == 0 || bq == ny) ? 1 : 2;
+
+        // B fragments, split once: entry (kt, tile, lane), tile 0 = Xr,
+        // 1 = Xi, 2 = Xr + Xi; fragment column gg = 4 rhs + point
+        const uint32_t sXq = sX + stage * P::X_BYTES;
+        for (int e = tid; e < P::KT * 32; e += P::THREADS) {
+            const int ln = e & 31, kt = e >> 5;
+            const int gg = ln >> 2, tt = ln & 3;
+            const int v = gg & 3, r = gg >> 2, mx = v >> 1, my = v & 1;
+            const bool present = mx < nkx && my < nky;
+            uint32_t w[12];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int k = 8 * kt + tt + 4 * h;
+                float2 x = make_float2(0.f, 0.f);
+                if (present) {
+                    x = lds64(sXq + (uint32_t)(v * P::XB + r * R + k) * 8u);
+                    const int comp = k / NZ;
+                    if ((comp == 0 && mx) || (comp == 1 && my)) x = make_float2(-x.x, -x.y);
+                }
+                split_rn(x.x, w[h], w[2 + h]);
+                split_rn(x.y, w[4 + h], w[6 + h]);
+                split_rn(x.x + x.y, w[8 + h], w[10 + h]);
+            }
+            const uint32_t base = sBF + (uint32_t)(kt * 3) * 512u + ln * 16u;
+            sts128(base, make_uint4(w[0], w[1], w[2], w[3]));
+            sts128(base + 512u, make_uint4(w[4], w[5], w[6], w[7]));
+            sts128(base + 1024u, make_uint4(w[8], w[9], w[10], w[11]));
+        }
+        __syncthreads();
+
+        float acc[MPW][3][4];
+#pragma unroll
+        for (int im = 0; im < MPW; im++)
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[im][j][c] = 0.f;
+        const float2 *Gq = reinterpret_cast<const float2 *>(smem + stage * P::G_BYTES);
+        const uint4 *BFq = reinterpret_cast<const uint4 *>(smem + P::OFF_BF) + lane;
+#pragma unroll
+        for (int ik = 0; ik < KMAX; ik++) {
+            if (ik >= kcnt) break;
+            const int kt = ktb + ik;
+            // the -A^T tiles: z rows (row group 2) x x|y columns
+            const uint32_t bsign = (mg == 2 && kt < 2 * NZ / 8) ? 0x80000000u : 0u;
+            uint4 b[3];
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                b[j] = BFq[(kt * 3 + j) * 32];
+                b[j].x ^= bsign;
+                b[j].y ^= bsign;
+                b[j].z ^= bsign;
+                b[j].w ^= bsign;
+            }
+#pragma unroll
+            for (int im = 0; im < MPW; im++) {
+                // [Gr hi, Gr lo, Gi hi, Gi lo, Gs hi, Gs lo][e]
+                uint32_t af[6][4];
+                const uint32_t t0 = tab[(im * KMAX + ik) * 2], t1 = tab[(im * KMAX + ik) * 2 + 1];
+                const uint32_t off[4] = {t0 & 0xffffu, t0 >> 16, t1 & 0xffffu, t1 >> 16};
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const float2 gv = Gq[off[e]];
+                    split(gv.x, af[0][e], af[1][e]);
+                    split(gv.y, af[2][e], af[3][e]);
+                    split(gv.x + gv.y, af[4][e], af[5][e]);
+                }
+                // three independent accumulator chains per row tile
+#pragma unroll
+                for (int j = 0; j < 3; j++) mma_tf32(acc[im][j], af[2 * j], b[j].x, b[j].y);
+#pragma unroll
+                for (int j = 0; j < 3; j++) mma_tf32(acc[im][j], af[2 * j], b[j].z, b[j].w);
+#pragma unroll
+                for (int j = 0; j < 3; j++) mma_tf32(acc[im][j], af[2 * j + 1], b[j].x, b[j].y);
+            }
+        }
+        // partial sums [kg][mt][re|im][c][lane]
+        float *PART =
+            reinterpret_cast<float *>(smem + (P::PART_IN_G ? stage * P::G_BYTES : P::OFF_BF + P::BF_BYTES)) + lane;
+        if (P::PART_IN_G) __syncthreads();  // every warp is done with the stage's block
+#pragma unroll
+        for (int im = 0; im < MPW; im++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const float t1 = acc[im][0][c], t2 = acc[im][1][c], t3 = acc[im][2][c];
+                const int base = ((kg * P::MT + mg * MPW + im) * 2) * 4 + c;
+                PART[base * 32] = t1 - t2;
+                PART[(base + 4) * 32] = t3 - t1 - t2;
+            }
+        __syncthreads();  // all partials are written
+        if (!P::PART_IN_G && tid == 0 && q + 2L * gridDim.x < Q) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(q + 2L * gridDim.x, stage);
+        }
+        // warp w < MT adds the column groups' partials of row tile w and stores
+        if (warp < P::MT) {
+            const int mt = warp;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                float yr = 0.f, yi = 0.f;
+#pragma unroll
+                for (int k = 0; k < P::KG; k++) {
+                    const int base = ((k * P::MT + mt) * 2) * 4 + c;
+                    yr += PART[base * 32];
+                    yi += PART[(base + 4) * 32];
+                }
+                // C: rows g, g+8; column 2t + (c & 1) = 4 rhs + point
+                const int row = 16 * mt + g + 8 * (c >> 1);
+                const int col = 2 * t + (c & 1), v = col & 3, r = col >> 2;
+                const int mx = v >> 1, my = v & 1;
+                if (mx < nkx && my < nky) {
+                    float2 val = make_float2(yr, yi);
+                    const int comp = row / NZ;
+                    if ((comp == 0 && mx) || (comp == 1 && my)) val = make_float2(-val.x, -val.y);
+                    const long pt = (long)(mx ? 2 * nx - a : a) * n1 + (my ? 2 * ny - bq : bq);
+                    buf[pt * B + (long)(rhs0 + r) * R + row] = val;
+                }
+            }
+        }
+        if (P::PART_IN_G) {
+            __syncthreads();  // the reduction has read the partials out of the stage
+            if (tid == 0 && q + 2L * gridDim.x < Q) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(q + 2L * gridDim.x, stage);
+            }
+        }
+    }
+}
+
+template <int NZ>
+void launch_sb3(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err, cudaStream_t s, int nsm) {
+    using P = Sb3<NZ>;
+    static bool attr = false;
+    if (!attr) {
+        EGX_CUDA(cudaFuncSetAttribute((const void *)k_contract_sb3<NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)P::SMEM));
+        attr = true;
+    }
+    const long Q = (long)(d.nx + 1) * (d.ny + 1);
+    const unsigned grid = (unsigned)std::min<long>(Q, nsm);
+    k_contract_sb3<NZ><<<grid, P::THREADS, P::SMEM, s>>>(buf, G, d.nx, d.ny, d.B, rhs0, err);
+    EGX_CUDA(cudaGetLastError());
+}
+
 template <int NZ, int NRHS>
 void launch_sb(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err, cudaStream_t s, int nsm) {
     using P = Sb<NZ, NRHS>;
@@ -449,7 +710,7 @@ template <int NZ>
 void launch_nz(float2 *buf, const float2 *G, const OpDims &d, int *err, cudaStream_t s, int nsm, long *launches) {
     for (int r0 = 0; r0 < d.nrhs;) {
         if (d.nrhs - r0 >= 2) {
-            launch_sb<NZ, 2>(buf, G, d, r0, err, s, nsm);
+            launch_sb3<NZ>(buf, G, d, r0, err, s, nsm);
             r0 += 2;
         } else {
             launch_sb<NZ, 1>(buf, G, d, r0, err, s, nsm);
