@@ -51,17 +51,45 @@ __device__ double block_sum(double v) {
     return v;
 }
 
+// Each thread keeps the partial sums of up to kDotCols columns in
+// registers, so w is read once per kDotCols columns (the stacked vectors are
+// larger than L2).
+constexpr int kDotCols = 16;
 template <typename T>
 __global__ void k_multi_dot(const C<T> *__restrict__ V, int ncols, const C<T> *__restrict__ w, long n,
                             double2 *__restrict__ partials) {
     const long stride = (long)gridDim.x * blockDim.x;
-    for (int k = 0; k < ncols; k++) {
-        const C<T> *col = V + (long)k * n;
-        C<T> acc = mk<T>(0, 0);
-        for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride)
-            cfma_conj<T>(acc, col[r], w[r]);
-        double2 s = block_sum2(make_double2((double)acc.x, (double)acc.y));
-        if (threadIdx.x == 0) partials[(long)blockIdx.x * ncols + k] = s;
+    for (int k0 = 0; k0 < ncols; k0 += kDotCols) {
+        const int kc = min(kDotCols, ncols - k0);
+        const C<T> *col = V + (long)k0 * n;
+        C<T> acc[kDotCols];
+#pragma unroll
+        for (int j = 0; j < kDotCols; j++) acc[j] = mk<T>(0, 0);
+        // two rows per thread and pass: twice the loads in flight
+        long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+        for (; r + stride < n; r += 2 * stride) {
+            const C<T> x0 = w[r], x1 = w[r + stride];
+#pragma unroll
+            for (int j = 0; j < kDotCols; j++)
+                if (j < kc) {
+                    const C<T> a0 = col[(long)j * n + r], a1 = col[(long)j * n + r + stride];
+                    cfma_conj<T>(acc[j], a0, x0);
+                    cfma_conj<T>(acc[j], a1, x1);
+                }
+        }
+        if (r < n) {
+            const C<T> x = w[r];
+#pragma unroll
+            for (int j = 0; j < kDotCols; j++)
+                if (j < kc) cfma_conj<T>(acc[j], col[(long)j * n + r], x);
+        }
+#pragma unroll
+        for (int j = 0; j < kDotCols; j++) {
+            if (j < kc) {  // kc is the same in every thread: the block sums stay uniform
+                double2 s = block_sum2(make_double2((double)acc[j].x, (double)acc[j].y));
+                if (threadIdx.x == 0) partials[(long)blockIdx.x * ncols + k0 + j] = s;
+            }
+        }
     }
 }
 
@@ -321,15 +349,14 @@ double Gmres<T>::arnoldi(double bn, int &jh) {
     const int m = m_;
     do {
         C<T> *vj = V_ + (long)jh * n_;
+        // w = A M v_j straight into w (the apply leaves its input unchanged)
         if (precond) {
             C<T> *zj = Z_ + (long)jh * n_;
             precond(vj, zj);
-            VecOps<T>::copy(zj, w_, n_, s_);
+            apply(zj, w_);
         } else {
-            VecOps<T>::copy(vj, w_, n_, s_);
+            apply(vj, w_);
         }
-        apply(w_, r0_);
-        VecOps<T>::copy(r0_, w_, n_, s_);
         for (int j = 0; j <= jh; j++) h(j, jh) = 0.0;
         int northo = 0;
         double dloo = 0, dnormw = 0;
