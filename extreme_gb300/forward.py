@@ -64,6 +64,16 @@ class LevelResult:
     impedance: np.ndarray  # [nx*ny, 2, 2]
     rho: np.ndarray        # [nx*ny, 2, 2] apparent resistivity, Ohm m
     phase: np.ndarray      # [nx*ny, 2, 2] degrees
+    e_anomaly: Optional[np.ndarray] = None  # [2 pols, nx, ny, 3] anomalous E
+    h_anomaly: Optional[np.ndarray] = None  # [2 pols, nx, ny, 3] anomalous H
+    e_normal: complex = 0j                  # plane-wave E0 at z (pol X: (E0, 0, 0), pol Y: (0, E0, 0))
+    h_normal: complex = 0j                  # plane-wave H0 at z (pol X: (0, H0, 0), pol Y: (-H0, 0, 0))
+
+    def normal_fields(self):
+        """Normal E and H of both polarisations at every site: [2, 3] each."""
+        en = np.array([[self.e_normal, 0, 0], [0, self.e_normal, 0]], complex)
+        hn = np.array([[0, self.h_normal, 0], [-self.h_normal, 0, 0]], complex)
+        return en, hn
 
 
 def model_zeta(model: CartesianModel, omega: float):
@@ -102,7 +112,7 @@ class Mt3DForwardSolver:
         e[1, ..., 1] += e_n   # pol Y: E = (0, E0, 0), H = (-H0, 0, 0)
         h[1, ..., 0] -= h_n
         imp, rho, ph = egx.mt_responses(e[0], e[1], h[0], h[1], omega)
-        return LevelResult(z, shift_x, shift_y, e, h, imp, rho, ph)
+        return LevelResult(z, shift_x, shift_y, e, h, imp, rho, ph, ea, ha, e_n, h_n)
 
     def solve(self, model: CartesianModel, frequency: float, green=None, want_chi=False,
               levels=()) -> MtSolution:
