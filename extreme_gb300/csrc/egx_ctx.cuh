@@ -56,8 +56,21 @@ struct egx_ctx {
     egx::DevBuf js, chi0;
     egx::DevBuf errflag;  // device int: EGX_ERR_TIMEOUT from a bounded wait
     egx::GreenBuildStats last_build;
-    // observation level: E and H level tensors, transformed sources, 3-column results
-    egx::DevBuf lvl_g[2], lvl_x, lvl_out, lvl_in, lvl_field;
+    // observation level: transformed sources, 3-column results
+    egx::DevBuf lvl_x, lvl_out, lvl_in, lvl_field;
+    // E and H level tensors of the most recently used levels, keyed by all
+    // they depend on (geometry, background, omega, filter length, level);
+    // the anomaly conductivity is not part of them
+    struct LevelEntry {
+        std::vector<double> key;
+        egx::DevBuf g[2];
+        unsigned long long used = 0;
+    };
+    static constexpr int kLevelSlots = 4;
+    LevelEntry lvl_cache[kLevelSlots];
+    int lvl_capacity = kLevelSlots;
+    unsigned long long lvl_clock = 0;
+    long lvl_hits = 0, lvl_builds = 0;
 };
 
 namespace egx {

@@ -114,8 +114,33 @@ int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_h
         const int nx = gm.nx, ny = gm.ny, nz = gm.nz, n0 = 2 * nx, n1 = 2 * ny, per = 3 * nz;
         cudaStream_t s = ctx->stream;
         ensure_twiddles(ctx, n0, n1);
-        build_level_green(gm, n_hankels, z, shift_x, shift_y, 0, s, ctx->lvl_g[0], &ctx->launches, ctx->gws);
-        build_level_green(gm, n_hankels, z, shift_x, shift_y, 1, s, ctx->lvl_g[1], &ctx->launches, ctx->gws);
+        // level tensors: reuse a cached pair or build into the least recently used slot
+        std::vector<double> key = {(double)nx, (double)ny, (double)nz, model->dx, model->dy, omega,
+                                   (double)n_hankels, z, shift_x, shift_y, (double)model->n_bg, model->zero_air_level};
+        key.insert(key.end(), model->layer_depth, model->layer_depth + nz);
+        key.insert(key.end(), model->layer_thickness, model->layer_thickness + nz);
+        key.insert(key.end(), model->bg_thickness, model->bg_thickness + model->n_bg);
+        key.insert(key.end(), model->bg_sigma, model->bg_sigma + model->n_bg);
+        const int cap = std::max(1, ctx->lvl_capacity);
+        int slot = -1;
+        if (ctx->lvl_capacity > 0)
+            for (int i = 0; i < cap; i++)
+                if (ctx->lvl_cache[i].key == key) slot = i;
+        if (slot >= 0) {
+            ctx->lvl_hits++;
+        } else {
+            slot = 0;
+            for (int i = 1; i < cap; i++)
+                if (ctx->lvl_cache[i].used < ctx->lvl_cache[slot].used) slot = i;
+            egx_ctx::LevelEntry &L = ctx->lvl_cache[slot];
+            L.key.clear();  // not valid until both tensors are built
+            build_level_green(gm, n_hankels, z, shift_x, shift_y, 0, s, L.g[0], &ctx->launches, ctx->gws);
+            build_level_green(gm, n_hankels, z, shift_x, shift_y, 1, s, L.g[1], &ctx->launches, ctx->gws);
+            if (ctx->lvl_capacity > 0) L.key = key;
+            ctx->lvl_builds++;
+        }
+        egx_ctx::LevelEntry &lv = ctx->lvl_cache[slot];
+        lv.used = ++ctx->lvl_clock;
         const long N = (long)nx * ny * per, P = (long)n0 * n1, F = (long)nx * ny * 3;
         ctx->lvl_x.ensure((size_t)P * per * sizeof(double2));
         ctx->lvl_out.ensure((size_t)P * 3 * sizeof(double2));
@@ -140,7 +165,7 @@ int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_h
             fft_lines<double>(X, nx, (long)n1 * per, per, per, ny, n1, ctx->p1, tw1, -1, s, &ctx->launches);
             fft_lines<double>(X, n1, per, (long)n1 * per, per, nx, n0, ctx->p0, tw0, -1, s, &ctx->launches);
             for (int kind = 0; kind < 2; kind++) {
-                k_level_contract<<<(unsigned)((P + 7) / 8), 256, 0, s>>>(X, ctx->lvl_g[kind].as<double2>(), P, nz,
+                k_level_contract<<<(unsigned)((P + 7) / 8), 256, 0, s>>>(X, lv.g[kind].as<double2>(), P, nz,
                                                                          kind, O);
                 EGX_CUDA(cudaGetLastError());
                 // inverse DFT of the 3 columns: x keeping rows < nx, then y keeping j < ny
@@ -163,6 +188,27 @@ int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_h
     } catch (const std::exception &err) {
         return fail(ctx, EGX_ERR_INVALID, err.what());
     }
+    return EGX_OK;
+}
+
+int egx_level_cache(egx_ctx *ctx, int capacity, long *hits, long *builds) {
+    if (!ctx) return EGX_ERR_INVALID;
+    if (capacity > egx_ctx::kLevelSlots) return fail(ctx, EGX_ERR_INVALID, "level cache holds at most 4 levels");
+    if (capacity >= 0) {
+        try {
+            set_device(ctx);
+        } catch (const egx::Error &err) {
+            return fail(ctx, err.code, err.what());
+        }
+        for (auto &L : ctx->lvl_cache) L.key.clear();
+        for (int i = std::max(1, capacity); i < egx_ctx::kLevelSlots; i++) {
+            ctx->lvl_cache[i].g[0].release();
+            ctx->lvl_cache[i].g[1].release();
+        }
+        ctx->lvl_capacity = capacity;
+    }
+    if (hits) *hits = ctx->lvl_hits;
+    if (builds) *builds = ctx->lvl_builds;
     return EGX_OK;
 }
 

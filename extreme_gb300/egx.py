@@ -26,7 +26,7 @@ EXPORTS = [
     "egx_op_prepare", "egx_op_apply", "egx_op_apply_c64", "egx_fft2d",
     "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products", "egx_dot_products_static",
     "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_read",
-    "egx_level_fields", "egx_mt_responses",
+    "egx_level_fields", "egx_level_cache", "egx_mt_responses",
 ]
 
 # kernel kinds of egx_profile_read
@@ -114,6 +114,7 @@ def load(path=None):
                                       C.POINTER(Result), i]
     lib.egx_level_fields.argtypes = [vp, C.POINTER(Model), d, i, d, d, d, vp, i, vp, vp, i]
     lib.egx_mt_responses.argtypes = [vp, vp, vp, vp, C.c_long, d, vp, vp, vp]
+    lib.egx_level_cache.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_long)]
     lib.egx_profile.argtypes = [vp, i]
     lib.egx_profile_read.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_double)]
     _lib = lib
@@ -309,6 +310,13 @@ class Context:
         if rc not in (OK, ERR_NOT_CONVERGED):
             self._check(rc)
         return jq, chi, [r.as_dict() for r in res]
+
+    def level_cache(self, capacity=-1):
+        """Set the level-tensor cache capacity (0..4; -1 keeps it) and return
+        (hits, builds) since the context was created (egx_level_cache)."""
+        hits, builds = C.c_long(), C.c_long()
+        self._check(self.lib.egx_level_cache(self.h, int(capacity), C.byref(hits), C.byref(builds)))
+        return hits.value, builds.value
 
     def level_fields(self, model, omega, jq, z=0.0, shift_x=0.0, shift_y=0.0, n_hankels=10):
         """Anomalous E and H at the observation level z for jq [nsrc, N]

@@ -43,6 +43,44 @@ class MixedSettings:
     batch: bool = True        # both polarisations as one stacked system
 
 
+class TensorCache:
+    """Green tensors kept across solves whose geometry and background do not
+    change, e.g. the forward solves of an inversion where only the anomaly
+    conductivity moves (``Extreme.Cartesian/Forward/TensorCache.cs:8-35``,
+    used by ``Mt3DForwardSolver.SolveWithoutGather``,
+    ``Mt3DForwardSolver.cs:85-110``): the anomaly-to-anomaly tensor per
+    (lateral geometry, anomaly layers, background, frequency, filter length,
+    precision). The level tensors are cached inside the context
+    (``Context.level_cache``). ``free()`` releases the device memory."""
+
+    def __init__(self):
+        self._atoa = {}
+
+    @staticmethod
+    def key(model: CartesianModel, frequency, n_hankels, precision):
+        sec = model.section
+        return (model.nx, model.ny, float(model.dx), float(model.dy), tuple(np.asarray(model.layer_depth, float)),
+                tuple(np.asarray(model.layer_thickness, float)), float(sec.zero_air_level),
+                tuple(np.asarray(sec.thickness, float)), tuple(np.asarray(sec.sigma, float)), float(frequency),
+                int(n_hankels), int(precision))
+
+    def atoa(self, solver, model: CartesianModel, frequency):
+        k = self.key(model, frequency, solver.settings.number_of_hankels, solver.precision)
+        g = self._atoa.get(k)
+        if g is None:
+            g = solver.calculate_green_tensor(model, frequency)
+            self._atoa[k] = g
+        return g
+
+    def __len__(self):
+        return len(self._atoa)
+
+    def free(self):
+        for g in self._atoa.values():
+            g.free()
+        self._atoa.clear()
+
+
 @dataclass
 class MtSolution:
     frequency: float
@@ -115,10 +153,14 @@ class Mt3DForwardSolver:
         return LevelResult(z, shift_x, shift_y, e, h, imp, rho, ph, ea, ha, e_n, h_n)
 
     def solve(self, model: CartesianModel, frequency: float, green=None, want_chi=False,
-              levels=()) -> MtSolution:
+              levels=(), tensors: Optional[TensorCache] = None) -> MtSolution:
         """Both polarisations to jQ; then, for every level (a depth or a
-        (depth, shift_x, shift_y) tuple), fields and responses."""
+        (depth, shift_x, shift_y) tuple), fields and responses. With
+        ``tensors`` the anomaly-to-anomaly Green tensor comes from (and stays
+        in) that cache."""
         omega = freq_to_omega(frequency)
+        if green is None and tensors is not None:
+            green = tensors.atoa(self, model, frequency)
         own = green is None
         if own:
             green = self.calculate_green_tensor(model, frequency)

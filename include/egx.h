@@ -215,6 +215,17 @@ int egx_solve_sources(egx_ctx *ctx, egx_green *g, const double *zeta, const doub
  * complex, anomalous part only (the normal field is egx_plane_wave at z). */
 int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_hankels, double z, double shift_x,
                      double shift_y, const double *jq, int nsrc, double *e, double *h, int where);
+/* Level-tensor cache of a context (the level part of TensorCache,
+ * Extreme.Cartesian/Forward/TensorCache.cs:8-35): egx_level_fields keeps the
+ * E and H level tensors of the last `capacity` levels (0..4, default 4),
+ * keyed by everything they depend on -- lateral geometry, anomaly layers,
+ * background section, omega, filter length, z and shifts, not the anomaly
+ * conductivity -- and reuses them when a later call matches. Each cached
+ * level holds 15 complex128 arrays of [2nx][2ny][nz] (3 GB at 256x256x48).
+ * capacity 0 rebuilds every call; a negative capacity leaves the setting;
+ * setting it drops the cached levels. hits, builds (may be NULL): counts of
+ * reused and built levels since the context was created. */
+int egx_level_cache(egx_ctx *ctx, int capacity, long *hits, long *builds);
 /* Impedance, apparent resistivity and phase at n sites from the total fields
  * of polarisation X (e1, h1) and Y (e2, h2), each [n][3] complex, host arrays
  * (ResponseFunctionsCalculator.CalculateTensor, ResponseFunctionsCalculator.cs:36-51;
