@@ -435,28 +435,33 @@ __global__ void __launch_bounds__(Sb<NZ, NRHS>::THREADS, 1)
 // Yi = T3 - T1 - T2. The eight columns of one n8 tile are the four points
 // sharing the stored block times the two right-hand sides (column 4 rhs + v),
 // so a (row tile, column tile) pair takes 3 products x 3 TF32 passes = 9 MMAs
-// where the embedded form takes 12. Each warp combines its partial sums to
-// (Yr, Yi) before the cross-warp reduction; when the partials do not fit
-// beside the other regions they reuse the stage's block buffer (free once
-// every warp is done with it) and the stage is refilled after the reduction.
+// where the embedded form takes 12.
+//
+// Each lane reads the two B values of its column straight from the staged
+// right-hand sides and splits them in registers (no separate B-fragment pass
+// and barrier). The eight (point, source) segments of a stage are copied
+// 32 bytes apart modulo 128, so one fragment load of a warp takes the
+// minimum two shared-memory wavefronts. Two block barriers per point: before
+// the partial sums are written (the previous reduction has read them) and
+// after (with the stage-wait status); then the stage is refilled and warps
+// w < MT reduce and store.
 template <int NZ>
 struct Sb3 {
     static constexpr int R = 3 * NZ, MT = R / 16, KT = R / 8, NB = NZ / 4;
     static constexpr int SYM = NB * (NB + 1) / 2 * 16, ASY = NB * NB * 16, BS = 4 * SYM + 2 * ASY;
     static constexpr int MG = 3, KG = 4, MPW = MT / MG, KMAX = (KT + KG - 1) / KG;
     static constexpr int THREADS = 32 * MG * KG;
-    static constexpr int XB = 2 * R;  // complex per spectral point (two right-hand sides)
+    static constexpr uint32_t SEG = R * 8u;        // bytes of one (point, source) segment
+    static constexpr uint32_t XS = SEG + 32u;      // its stride in a stage
     static constexpr uint32_t G_BYTES = BS * 8u;
-    static constexpr uint32_t X_BYTES = 4u * XB * 8u;
-    static constexpr uint32_t BF_BYTES = KT * 3u * 32u * 16u;
+    static constexpr uint32_t X_BYTES = 8u * XS;   // 4 points x 2 sources
     static constexpr uint32_t PART_BYTES = KG * MT * 2u * 4u * 32u * 4u;
-    static constexpr bool PART_IN_G = 2 * G_BYTES + 2 * X_BYTES + BF_BYTES + PART_BYTES > 227u * 1024u;
-    static constexpr uint32_t OFF_X = 2 * G_BYTES, OFF_BF = OFF_X + 2 * X_BYTES;
-    static constexpr uint32_t SMEM = PART_IN_G ? OFF_BF + BF_BYTES : OFF_BF + BF_BYTES + PART_BYTES;
+    static constexpr uint32_t OFF_X = 2 * G_BYTES, OFF_PART = OFF_X + 2 * X_BYTES;
+    static constexpr uint32_t SMEM = OFF_PART + PART_BYTES;
     static_assert(MT % MG == 0, "row tiles must split over the row groups");
-    static_assert(!PART_IN_G || PART_BYTES <= G_BYTES, "partials must fit in one block buffer");
+    static_assert(SMEM + 256 <= 227u * 1024u, "shared memory per block");
     static_assert(MT <= MG * KG, "one warp per row tile in the epilogue");
-    static_assert(G_BYTES % 128 == 0 && X_BYTES % 128 == 0, "stage alignment");
+    static_assert(G_BYTES % 128 == 0 && SEG % 16 == 0 && XS % 128 == 32, "stage alignment and bank skew");
     __host__ __device__ static constexpr int kt0(int kg) { return kg * KT / KG; }
 };
 
@@ -468,15 +473,16 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
     constexpr int R = P::R, MPW = P::MPW, KMAX = P::KMAX;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int status;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t = lane & 3;
     const int mg = warp % P::MG, kg = warp / P::MG;
     const int ktb = P::kt0(kg), kcnt = P::kt0(kg + 1) - ktb;
-    const uint32_t sG = saddr(smem), sX = sG + P::OFF_X, sBF = sG + P::OFF_BF;
+    const uint32_t sG = saddr(smem), sX = sG + P::OFF_X;
     const uint32_t bar0 = saddr(&bars[0]);
     const long Q = (long)(nx + 1) * (ny + 1);
     const int n1 = 2 * ny;
+    // this lane's B column: point v, source rb
+    const int bv = g & 3, brs = g >> 2, bmx = bv >> 1, bmy = bv & 1;
 
     // A-fragment offsets in registers, built through the stage-0 block buffer
     constexpr int TABN = MPW * KMAX * 2;
@@ -505,7 +511,6 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        status = 0;
     }
     __syncthreads();
 
@@ -514,13 +519,16 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
         const int nkx = (a == 0 || a == nx) ? 1 : 2;
         const int nky = (bq == 0 || bq == ny) ? 1 : 2;
         const uint32_t bar = bar0 + 8 * stage;
-        bar_expect(bar, P::G_BYTES + (uint32_t)(nkx * nky) * (P::XB * 8u));
+        bar_expect(bar, P::G_BYTES + (uint32_t)(nkx * nky) * (2u * P::SEG));
         bulk_g2s(sG + stage * P::G_BYTES, G + qq * P::BS, P::G_BYTES, bar);
         for (int p = 0; p < 4; p++) {
             const int mx = p >> 1, my = p & 1;
             if (mx < nkx && my < nky) {
                 const long pt = (long)(mx ? 2 * nx - a : a) * n1 + (my ? 2 * ny - bq : bq);
-                bulk_g2s(sX + stage * P::X_BYTES + p * (P::XB * 8u), buf + pt * B + (long)rhs0 * R, P::XB * 8u, bar);
+#pragma unroll
+                for (int r = 0; r < 2; r++)
+                    bulk_g2s(sX + stage * P::X_BYTES + (uint32_t)(p * 2 + r) * P::XS, buf + pt * B + (long)(rhs0 + r) * R,
+                             P::SEG, bar);
             }
         }
     };
@@ -530,52 +538,20 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
         if (q + gridDim.x < Q) issue(q + gridDim.x, 1);
     }
 
+    float *PART = reinterpret_cast<float *>(smem + P::OFF_PART) + lane;
     for (int it = 0; q < Q; q += gridDim.x, it++) {
         const int stage = it & 1;
         const uint32_t parity = (it >> 1) & 1;
         const uint32_t bar = bar0 + 8 * stage;
-        if (tid == 0 && !bar_wait(bar, parity, kWait)) status = 1;
-        __syncthreads();
-        if (status) {
-            if (tid == 0) {
-                atomicExch(err, EGX_ERR_TIMEOUT);
-                bar_wait(bar0 + 8 * (stage ^ 1), ((it + 1) >> 1) & 1, kWait);
-            }
-            return;
-        }
-        bar_wait(bar, parity, kWait);  // acquire the stage for every thread
+        // every thread acquires the stage itself (bounded); the barrier after
+        // the partial sums shares the outcome
+        const bool late = !bar_wait(bar, parity, kWait);
         const int a = (int)(q / (ny + 1)), bq = (int)(q - (long)a * (ny + 1));
         const int nkx = (a == 0 || a == nx) ? 1 : 2;
         const int nky = (bq == 0 || bq == ny) ? 1 : 2;
-
-        // B fragments, split once: entry (kt, tile, lane), tile 0 = Xr,
-        // 1 = Xi, 2 = Xr + Xi; fragment column gg = 4 rhs + point
-        const uint32_t sXq = sX + stage * P::X_BYTES;
-        for (int e = tid; e < P::KT * 32; e += P::THREADS) {
-            const int ln = e & 31, kt = e >> 5;
-            const int gg = ln >> 2, tt = ln & 3;
-            const int v = gg & 3, r = gg >> 2, mx = v >> 1, my = v & 1;
-            const bool present = mx < nkx && my < nky;
-            uint32_t w[12];
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int k = 8 * kt + tt + 4 * h;
-                float2 x = make_float2(0.f, 0.f);
-                if (present) {
-                    x = lds64(sXq + (uint32_t)(v * P::XB + r * R + k) * 8u);
-                    const int comp = k / NZ;
-                    if ((comp == 0 && mx) || (comp == 1 && my)) x = make_float2(-x.x, -x.y);
-                }
-                split_rn(x.x, w[h], w[2 + h]);
-                split_rn(x.y, w[4 + h], w[6 + h]);
-                split_rn(x.x + x.y, w[8 + h], w[10 + h]);
-            }
-            const uint32_t base = sBF + (uint32_t)(kt * 3) * 512u + ln * 16u;
-            sts128(base, make_uint4(w[0], w[1], w[2], w[3]));
-            sts128(base + 512u, make_uint4(w[4], w[5], w[6], w[7]));
-            sts128(base + 1024u, make_uint4(w[8], w[9], w[10], w[11]));
-        }
-        __syncthreads();
+        const bool bpresent = bmx < nkx && bmy < nky;
+        const float2 *xcol = reinterpret_cast<const float2 *>(smem + P::OFF_X + stage * P::X_BYTES +
+                                                              (uint32_t)(bv * 2 + brs) * P::XS);
 
         float acc[MPW][3][4];
 #pragma unroll
@@ -585,22 +561,32 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
 #pragma unroll
                 for (int c = 0; c < 4; c++) acc[im][j][c] = 0.f;
         const float2 *Gq = reinterpret_cast<const float2 *>(smem + stage * P::G_BYTES);
-        const uint4 *BFq = reinterpret_cast<const uint4 *>(smem + P::OFF_BF) + lane;
 #pragma unroll
         for (int ik = 0; ik < KMAX; ik++) {
             if (ik >= kcnt) break;
             const int kt = ktb + ik;
-            // the -A^T tiles: z rows (row group 2) x x|y columns
-            const uint32_t bsign = (mg == 2 && kt < 2 * NZ / 8) ? 0x80000000u : 0u;
-            uint4 b[3];
-#pragma unroll
-            for (int j = 0; j < 3; j++) {
-                b[j] = BFq[(kt * 3 + j) * 32];
-                b[j].x ^= bsign;
-                b[j].y ^= bsign;
-                b[j].z ^= bsign;
-                b[j].w ^= bsign;
+            // B values of rows 8kt + t and 8kt + t + 4 of this lane's column,
+            // with the D_p sign of their component and the sign of the -A^T
+            // tiles (z rows of row group 2 x x|y columns)
+            float2 x0 = make_float2(0.f, 0.f), x1 = make_float2(0.f, 0.f);
+            if (bpresent) {
+                x0 = xcol[8 * kt + t];
+                x1 = xcol[8 * kt + t + 4];
             }
+            const int comp = (8 * kt) / NZ;
+            const bool flip = ((comp == 0 && bmx) || (comp == 1 && bmy)) != (mg == 2 && comp < 2);
+            if (flip) {
+                x0 = make_float2(-x0.x, -x0.y);
+                x1 = make_float2(-x1.x, -x1.y);
+            }
+            // [Xr, Xi, Xr + Xi] x (hi b0, hi b1, lo b0, lo b1)
+            uint32_t b[3][4];
+            split_rn(x0.x, b[0][0], b[0][2]);
+            split_rn(x1.x, b[0][1], b[0][3]);
+            split_rn(x0.y, b[1][0], b[1][2]);
+            split_rn(x1.y, b[1][1], b[1][3]);
+            split_rn(x0.x + x0.y, b[2][0], b[2][2]);
+            split_rn(x1.x + x1.y, b[2][1], b[2][3]);
 #pragma unroll
             for (int im = 0; im < MPW; im++) {
                 // [Gr hi, Gr lo, Gi hi, Gi lo, Gs hi, Gs lo][e]
@@ -616,17 +602,15 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
                 }
                 // three independent accumulator chains per row tile
 #pragma unroll
-                for (int j = 0; j < 3; j++) mma_tf32(acc[im][j], af[2 * j], b[j].x, b[j].y);
+                for (int j = 0; j < 3; j++) mma_tf32(acc[im][j], af[2 * j], b[j][0], b[j][1]);
 #pragma unroll
-                for (int j = 0; j < 3; j++) mma_tf32(acc[im][j], af[2 * j], b[j].z, b[j].w);
+                for (int j = 0; j < 3; j++) mma_tf32(acc[im][j], af[2 * j], b[j][2], b[j][3]);
 #pragma unroll
-                for (int j = 0; j < 3; j++) mma_tf32(acc[im][j], af[2 * j + 1], b[j].x, b[j].y);
+                for (int j = 0; j < 3; j++) mma_tf32(acc[im][j], af[2 * j + 1], b[j][0], b[j][1]);
             }
         }
+        __syncthreads();  // the previous point's reduction has read the partial sums
         // partial sums [kg][mt][re|im][c][lane]
-        float *PART =
-            reinterpret_cast<float *>(smem + (P::PART_IN_G ? stage * P::G_BYTES : P::OFF_BF + P::BF_BYTES)) + lane;
-        if (P::PART_IN_G) __syncthreads();  // every warp is done with the stage's block
 #pragma unroll
         for (int im = 0; im < MPW; im++)
 #pragma unroll
@@ -636,8 +620,14 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
                 PART[base * 32] = t1 - t2;
                 PART[(base + 4) * 32] = t3 - t1 - t2;
             }
-        __syncthreads();  // all partials are written
-        if (!P::PART_IN_G && tid == 0 && q + 2L * gridDim.x < Q) {
+        if (__syncthreads_or(late)) {  // partials written; the stage is free
+            if (tid == 0) {
+                atomicExch(err, EGX_ERR_TIMEOUT);
+                bar_wait(bar0 + 8 * (stage ^ 1), ((it + 1) >> 1) & 1, kWait);
+            }
+            return;
+        }
+        if (tid == 0 && q + 2L * gridDim.x < Q) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(q + 2L * gridDim.x, stage);
         }
@@ -664,13 +654,6 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
                     const long pt = (long)(mx ? 2 * nx - a : a) * n1 + (my ? 2 * ny - bq : bq);
                     buf[pt * B + (long)(rhs0 + r) * R + row] = val;
                 }
-            }
-        }
-        if (P::PART_IN_G) {
-            __syncthreads();  // the reduction has read the partials out of the stage
-            if (tid == 0 && q + 2L * gridDim.x < Q) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue(q + 2L * gridDim.x, stage);
             }
         }
     }
