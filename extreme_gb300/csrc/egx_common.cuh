@@ -2,6 +2,10 @@
 // double2/float2, error handling, the context object.
 #pragma once
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
@@ -138,6 +142,24 @@ struct Timers {
 };
 
 // Device buffer owned by the context.
+// Raise a kernel's dynamic shared-memory limit to at least `bytes` on the
+// current device; never lower it. The limit belongs to the kernel, not to a
+// context: contexts on other host threads may launch the same kernel with a
+// larger size at any moment, so a per-launch set to the launch's own size
+// would race with them.
+inline void raise_smem_limit(const void *fn, size_t bytes) {
+    if (bytes <= 48 * 1024) return;
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, size_t> limits;
+    int dev = 0;
+    EGX_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cur = limits[std::make_pair(fn, dev)];
+    if (bytes <= cur) return;
+    EGX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
+}
+
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;

@@ -330,12 +330,10 @@ void launch_contract_c64(float2 *buf, const float2 *G, const OpDims &d, int *err
     const size_t sm = contract_c64_smem(d.nz, d.nrhs);
     const unsigned grid = (unsigned)std::min<long>(gd.Q(), nsm);
     if (d.nrhs == 1) {
-        EGX_CUDA(cudaFuncSetAttribute((const void *)k_contract_c64<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sm));
+        raise_smem_limit((const void *)k_contract_c64<1>, sm);
         k_contract_c64<1><<<grid, thr, sm, s>>>(buf, G, d, err);
     } else {
-        EGX_CUDA(cudaFuncSetAttribute((const void *)k_contract_c64<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sm));
+        raise_smem_limit((const void *)k_contract_c64<2>, sm);
         k_contract_c64<2><<<grid, thr, sm, s>>>(buf, G, d, err);
     }
     EGX_CUDA(cudaGetLastError());

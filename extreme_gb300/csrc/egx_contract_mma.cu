@@ -314,7 +314,7 @@ void launch_contract_mma(float2 *buf, const float2 *G, const OpDims &d, int *err
     const size_t sm = contract_mma_smem(d.nz, d.nrhs);
     const unsigned grid = (unsigned)std::min<long>(gd.Q(), nsm);
     const int thr = std::max(64, m.MT * 32);
-    EGX_CUDA(cudaFuncSetAttribute((const void *)k_contract_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    raise_smem_limit((const void *)k_contract_mma, sm);
     k_contract_mma<<<grid, thr, sm, s>>>(buf, G, d, err);
     EGX_CUDA(cudaGetLastError());
 }

@@ -662,12 +662,7 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
 template <int NZ>
 void launch_sb3(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err, cudaStream_t s, int nsm) {
     using P = Sb3<NZ>;
-    static bool attr = false;
-    if (!attr) {
-        EGX_CUDA(cudaFuncSetAttribute((const void *)k_contract_sb3<NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)P::SMEM));
-        attr = true;
-    }
+    raise_smem_limit((const void *)k_contract_sb3<NZ>, P::SMEM);
     const long Q = (long)(d.nx + 1) * (d.ny + 1);
     const unsigned grid = (unsigned)std::min<long>(Q, nsm);
     k_contract_sb3<NZ><<<grid, P::THREADS, P::SMEM, s>>>(buf, G, d.nx, d.ny, d.B, rhs0, err);
@@ -677,12 +672,7 @@ void launch_sb3(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *er
 template <int NZ, int NRHS>
 void launch_sb(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err, cudaStream_t s, int nsm) {
     using P = Sb<NZ, NRHS>;
-    static bool attr = false;
-    if (!attr) {
-        EGX_CUDA(cudaFuncSetAttribute((const void *)k_contract_sb<NZ, NRHS>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM));
-        attr = true;
-    }
+    raise_smem_limit((const void *)k_contract_sb<NZ, NRHS>, P::SMEM);
     const long Q = (long)(d.nx + 1) * (d.ny + 1);
     const unsigned grid = (unsigned)std::min<long>(Q, nsm);
     k_contract_sb<NZ, NRHS><<<grid, P::THREADS, P::SMEM, s>>>(buf, G, d.nx, d.ny, d.B, rhs0, err);

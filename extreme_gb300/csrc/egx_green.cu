@@ -24,6 +24,8 @@
 #include <chrono>
 #include <cmath>
 #include <complex>
+#include <mutex>
+#include <set>
 
 #include "egx_green.cuh"
 #include "egx_operator.cuh"
@@ -969,6 +971,21 @@ std::vector<int> background_indices(const GreenModel &m) {
     return out;
 }
 
+
+// The filter taps in constant memory, once per device (contexts on other
+// host threads may build at the same time).
+static void load_hankel_taps() {
+    static std::mutex mu;
+    static std::set<int> loaded;
+    int dev = 0;
+    EGX_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (loaded.count(dev)) return;
+    EGX_CUDA(cudaMemcpyToSymbol(c_h0, kHankelJ0, sizeof(kHankelJ0)));
+    EGX_CUDA(cudaMemcpyToSymbol(c_h1, kHankelJ1, sizeof(kHankelJ1)));
+    loaded.insert(dev);
+}
+
 void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &quad, GreenBuildStats *stats,
                  long *launches, Timers *tm, GreenWorkspace *ws) {
     auto t_start = std::chrono::steady_clock::now();
@@ -977,12 +994,7 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
     EGX_CHECK(L >= 3 && L <= kMaxLayers, EGX_ERR_INVALID, "background must have 3.." + std::to_string(kMaxLayers) +
                                                               " layers including both half-spaces");
     background_indices(m);
-    static bool taps_loaded = false;
-    if (!taps_loaded) {
-        EGX_CUDA(cudaMemcpyToSymbol(c_h0, kHankelJ0, sizeof(kHankelJ0)));
-        EGX_CUDA(cudaMemcpyToSymbol(c_h1, kHankelJ1, sizeof(kHankelJ1)));
-        taps_loaded = true;
-    }
+    load_hankel_taps();
     // ---- background
     LayerArgs la{};
     la.L = L;
@@ -1239,12 +1251,7 @@ void build_level_green(const GreenModel &m, int n_hankels, double z, double shx,
     const int L = (int)m.bg_thick.size();
     EGX_CHECK(L >= 3 && L <= kMaxLayers, EGX_ERR_INVALID, "background must have 3.." + std::to_string(kMaxLayers) +
                                                               " layers including both half-spaces");
-    static bool taps_loaded = false;
-    if (!taps_loaded) {
-        EGX_CUDA(cudaMemcpyToSymbol(c_h0, kHankelJ0, sizeof(kHankelJ0)));
-        EGX_CUDA(cudaMemcpyToSymbol(c_h1, kHankelJ1, sizeof(kHankelJ1)));
-        taps_loaded = true;
-    }
+    load_hankel_taps();
     // ---- background (as build_green)
     LayerArgs la{};
     la.L = L;

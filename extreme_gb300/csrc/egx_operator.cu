@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(reg_threads<N, T>())
 template <typename T, int N>
 static void reg_attr(const void *fn) {
     constexpr size_t sm = reg_smem<N, T>();
-    if (sm > 48 * 1024) EGX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    raise_smem_limit(fn, sm);
 }
 
 // which: 0 fwd_y, 1 lines, 2 bwd_y
@@ -229,16 +229,13 @@ static void launch_reg(int which, dim3 grid, cudaStream_t s, const C<T> *x, cons
     constexpr size_t sm = reg_smem<N, T>();
     constexpr int thr = reg_threads<N, T>();
     if (which == 0) {
-        static bool a = false;
-        if (!a) reg_attr<T, N>((const void *)k_fwd_y_r<T, N>), a = true;
+        reg_attr<T, N>((const void *)k_fwd_y_r<T, N>);
         k_fwd_y_r<T, N><<<grid, thr, sm, s>>>(x, *op, buf, *d, tw);
     } else if (which == 1) {
-        static bool a = false;
-        if (!a) reg_attr<T, N>((const void *)k_lines_r<T, N>), a = true;
+        reg_attr<T, N>((const void *)k_lines_r<T, N>);
         k_lines_r<T, N><<<grid, thr, sm, s>>>(buf, lstride, estride, B, nload, nstore, tw, sign);
     } else {
-        static bool a = false;
-        if (!a) reg_attr<T, N>((const void *)k_bwd_y_r<T, N>), a = true;
+        reg_attr<T, N>((const void *)k_bwd_y_r<T, N>);
         k_bwd_y_r<T, N><<<grid, thr, sm, s>>>(buf, x, *op, y, *d, tw);
     }
 }
@@ -344,7 +341,7 @@ static int threads_for(int items) { return items >= 256 ? 256 : (items >= 128 ? 
 
 template <typename T>
 static void set_smem(const void *fn, size_t bytes) {
-    if (bytes > 48 * 1024) EGX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    raise_smem_limit(fn, bytes);
 }
 
 template <typename T>
@@ -483,8 +480,7 @@ void fft_lines(C<T> *buf, int nlines, long lstride, long estride, int B, int nlo
 template <typename T, int N>
 static void launch_sym(dim3 grid, cudaStream_t s, C<T> *buf, long lstride, long estride, int B, T par, int nstore,
                        const C<T> *tw, int sign) {
-    static bool a = false;
-    if (!a) reg_attr<T, N>((const void *)k_lines_sym_r<T, N>), a = true;
+    reg_attr<T, N>((const void *)k_lines_sym_r<T, N>);
     k_lines_sym_r<T, N><<<grid, reg_threads<N, T>(), reg_smem<N, T>(), s>>>(buf, lstride, estride, B, par, nstore, tw,
                                                                             sign);
 }
