@@ -176,6 +176,8 @@ def run_ours(args, rank, world, local):
     # the library launches on this stream, so events recorded on it time its kernels
     stream = torch.cuda.Stream(dev)
     ctx.set_stream(stream.cuda_stream)
+    # every step builds its level tensors like a fresh solve: no reuse across steps
+    ctx.level_cache(0)
     n = m.nx * m.ny * 3 * m.nz
     mixed = dict(tol=1e-6, max_outer=5, m_out=30, m_in=10, inner_tol=5e-7, inner_restarts=20,
                  batch=not args.no_batch)
@@ -358,6 +360,7 @@ def run_ours(args, rank, world, local):
         "plain_fp64": plain,
         "clocks": clocks,
         "gpu_launches": launches,
+        "launches_before_timed": l0,
         "kernels": kernels,
         "step_ms": [round(t, 1) for t in step_ms],
         "solves": [[{k: r[k] for k in ("converged", "iterations", "n_applies", "n_refinements", "true_be")}
