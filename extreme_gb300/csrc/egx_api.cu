@@ -503,7 +503,9 @@ int egx_green_build(egx_ctx *ctx, const egx_model *model, double omega, int n_ha
         g->nz = gm.nz;
         GreenBuildStats st;
         g->g64.swap(ctx->spare64);  // storage of the last freed tensor, if any
-        build_green(gm, n_hankels, ctx->stream, g->g64, &st, &ctx->launches, &ctx->timers, &ctx->gws);
+        // the mixed form transforms the FP64 face integrals laterally in complex64
+        build_green(gm, n_hankels, ctx->stream, g->g64, &st, &ctx->launches, &ctx->timers, &ctx->gws,
+                    precision == EGX_PREC_MIXED);
         if (precision == EGX_PREC_MIXED) {
             GreenDims gd{gm.nx, gm.ny, gm.nz};
             g->g32.swap(ctx->spare32);

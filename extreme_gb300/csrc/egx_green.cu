@@ -342,11 +342,19 @@ struct Term {
     double wa, wb;
 };
 
+template <typename O> __device__ __forceinline__ O cell_out(double2 v);
+template <> __device__ __forceinline__ double2 cell_out<double2>(double2 v) { return v; }
+template <> __device__ __forceinline__ float2 cell_out<float2>(double2 v) {
+    return make_float2((float)v.x, (float)v.y);
+}
+
 // Real-space value of each quadrant cell for block entries [t0, t0+tc),
-// written with the parity mirroring into buf[2nx][2ny][tc].
+// written with the parity mirroring into buf[2nx][2ny][tc] (or only the
+// quadrant when compact), as complex128 or rounded to complex64.
+template <typename O>
 __global__ void k_cells(const int *__restrict__ rowptr, const Term *__restrict__ terms, const double2 *__restrict__ IA,
                         const double2 *__restrict__ IB, int ntrans, int nseg, int nx, int ny, int t0, int tc, int xs,
-                        int ys, int compact, double2 *__restrict__ buf) {
+                        int ys, int compact, O *__restrict__ buf) {
     const int cell = blockIdx.x;
     const int i = cell / ny, j = cell - (cell / ny) * ny;
     const int t = blockIdx.y * blockDim.x + threadIdx.x;
@@ -364,25 +372,26 @@ __global__ void k_cells(const int *__restrict__ rowptr, const Term *__restrict__
     if (compact) {
         // quadrant buffer [nx+1][ny+1][tc]: the mirror images are made by
         // the FFT's loads (fft_lines_sym)
-        buf[((long)i * (ny + 1) + j) * tc + t] = acc;
+        buf[((long)i * (ny + 1) + j) * tc + t] = cell_out<O>(acc);
         return;
     }
     const int n0 = 2 * nx, n1 = 2 * ny;
-    buf[((long)i * n1 + j) * tc + t] = acc;
+    buf[((long)i * n1 + j) * tc + t] = cell_out<O>(acc);
     if (i >= 1 && j >= 1) {
-        buf[((long)(n0 - i) * n1 + j) * tc + t] = dscal((double)xs, acc);
-        buf[((long)i * n1 + (n1 - j)) * tc + t] = dscal((double)ys, acc);
-        buf[((long)(n0 - i) * n1 + (n1 - j)) * tc + t] = dscal((double)(xs * ys), acc);
+        buf[((long)(n0 - i) * n1 + j) * tc + t] = cell_out<O>(dscal((double)xs, acc));
+        buf[((long)i * n1 + (n1 - j)) * tc + t] = cell_out<O>(dscal((double)ys, acc));
+        buf[((long)(n0 - i) * n1 + (n1 - j)) * tc + t] = cell_out<O>(dscal((double)(xs * ys), acc));
     } else if (i >= 1) {
-        buf[((long)(n0 - i) * n1) * tc + t] = dscal((double)xs, acc);
+        buf[((long)(n0 - i) * n1) * tc + t] = cell_out<O>(dscal((double)xs, acc));
     } else if (j >= 1) {
-        buf[((long)(n1 - j)) * tc + t] = dscal((double)ys, acc);
+        buf[((long)(n1 - j)) * tc + t] = cell_out<O>(dscal((double)ys, acc));
     }
 }
 
 // quad block entry of reference entry tt: packed symmetric entries keep
 // their index, xz/yz entries rc*nz + tr move to rc*(nz+1) + tr.
-__global__ void k_extract(const double2 *__restrict__ buf, int nx, int ny, int row, int tc, int Bs, int off, int t0,
+template <typename I>
+__global__ void k_extract(const I *__restrict__ buf, int nx, int ny, int row, int tc, int Bs, int off, int t0,
                           int nz, int asym, double2 *__restrict__ quad) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     long total = (long)(nx + 1) * (ny + 1) * tc;
@@ -392,7 +401,8 @@ __global__ void k_extract(const double2 *__restrict__ buf, int nx, int ny, int r
     int a = (int)(q / (ny + 1)), b = (int)(q - (long)a * (ny + 1));
     int tt = t0 + t;
     int dst = asym ? (tt / nz) * (nz + 1) + tt % nz : tt;
-    quad[q * Bs + off + dst] = buf[((long)a * row + b) * tc + t];
+    const I v = buf[((long)a * row + b) * tc + t];
+    quad[q * Bs + off + dst] = make_double2((double)v.x, (double)v.y);
 }
 
 // ---------------------------------------------------------------- host plan
@@ -987,7 +997,7 @@ static void load_hankel_taps() {
 }
 
 void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &quad, GreenBuildStats *stats,
-                 long *launches, Timers *tm, GreenWorkspace *ws) {
+                 long *launches, Timers *tm, GreenWorkspace *ws, bool lateral_fft32) {
     auto t_start = std::chrono::steady_clock::now();
     EGX_CHECK(m.nx > 0 && m.ny > 0 && m.nz > 0 && m.dx > 0 && m.dy > 0, EGX_ERR_INVALID, "bad model dimensions");
     const int L = (int)m.bg_thick.size();
@@ -1109,6 +1119,10 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
         std::vector<double> t0 = twiddles(2 * m.nx), t1 = twiddles(2 * m.ny);
         dev_upload(tw0, t0, s);
         dev_upload(tw1, t1, s);
+        if (lateral_fft32) {
+            dev_upload(w.tw0_32, std::vector<float>(t0.begin(), t0.end()), s);
+            dev_upload(w.tw1_32, std::vector<float>(t1.begin(), t1.end()), s);
+        }
     }
     double *radii_dev = dev_upload(d_radii, radii, s);
 
@@ -1181,10 +1195,14 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
         // otherwise the full 2nx x 2ny grid populated by mirroring
         const int n0 = 2 * m.nx, n1 = 2 * m.ny;
         const bool compact = fft_lines_sym_ok(n0) && fft_lines_sym_ok(n1);
+        const bool fft32 = lateral_fft32 && compact;
         const long cells4 = compact ? (long)(m.nx + 1) * (m.ny + 1) : 4L * m.nx * m.ny;
         const int row = compact ? m.ny + 1 : n1;
         int tc = (int)std::min<long>(blk, std::max<long>(1, (long)(1.5e9 / (cells4 * sizeof(double2)))));
-        d_buf.ensure((size_t)cells4 * tc * sizeof(double2));
+        if (fft32)
+            w.d_buf32.ensure((size_t)cells4 * tc * sizeof(float2));
+        else
+            d_buf.ensure((size_t)cells4 * tc * sizeof(double2));
         for (int ci = 0; ci < ncomp; ci++) {
             const int c = comps[ci];
             auto t_int = std::chrono::steady_clock::now();
@@ -1208,12 +1226,24 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
                 if (!compact) EGX_CUDA(cudaMemsetAsync(d_buf.p, 0, (size_t)cells4 * tcc * sizeof(double2), s));
                 dim3 grid(m.nx * m.ny, (tcc + 127) / 128);
                 int ev = tm ? tm->begin(EGX_K_GREEN_CELLS, s) : -1;
-                k_cells<<<grid, 128, 0, s>>>(drow, dterm, d_IA.as<double2>(), d_IB.as<double2>(), ntrans, nseg, m.nx,
-                                             m.ny, t0, tcc, px[c], py[c], compact ? 1 : 0, d_buf.as<double2>());
+                if (fft32)
+                    k_cells<float2><<<grid, 128, 0, s>>>(drow, dterm, d_IA.as<double2>(), d_IB.as<double2>(), ntrans,
+                                                         nseg, m.nx, m.ny, t0, tcc, px[c], py[c], 1,
+                                                         w.d_buf32.as<float2>());
+                else
+                    k_cells<double2><<<grid, 128, 0, s>>>(drow, dterm, d_IA.as<double2>(), d_IB.as<double2>(), ntrans,
+                                                          nseg, m.nx, m.ny, t0, tcc, px[c], py[c], compact ? 1 : 0,
+                                                          d_buf.as<double2>());
                 if (tm) tm->end(ev, s);
                 EGX_CUDA(cudaGetLastError());
                 ev = tm ? tm->begin(EGX_K_GREEN_FFT, s) : -1;
-                if (compact) {
+                if (fft32) {
+                    // as below, in complex64
+                    fft_lines_sym<float>(w.d_buf32.as<float2>(), m.nx, (long)row * tcc, tcc, tcc, py[c], m.ny + 1, n1,
+                                         w.tw1_32.as<float2>(), -1, s, launches);
+                    fft_lines_sym<float>(w.d_buf32.as<float2>(), m.ny + 1, tcc, (long)row * tcc, tcc, px[c], m.nx + 1,
+                                         n0, w.tw0_32.as<float2>(), -1, s, launches);
+                } else if (compact) {
                     // y along the nx computed rows, ky <= ny kept; then x along
                     // ky <= ny, kx <= nx kept (row nx of the input is zero)
                     fft_lines_sym<double>(d_buf.as<double2>(), m.nx, (long)row * tcc, tcc, tcc, py[c], m.ny + 1, n1,
@@ -1229,9 +1259,14 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
                 }
                 if (tm) tm->end(ev, s);
                 long n = (long)(m.nx + 1) * (m.ny + 1) * tcc;
-                k_extract<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_buf.as<double2>(), m.nx, m.ny, row, tcc, Bs,
-                                                                      offs[c], t0, m.nz, c >= 4 ? 1 : 0,
-                                                                      quad.as<double2>());
+                if (fft32)
+                    k_extract<float2><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+                        w.d_buf32.as<float2>(), m.nx, m.ny, row, tcc, Bs, offs[c], t0, m.nz, c >= 4 ? 1 : 0,
+                        quad.as<double2>());
+                else
+                    k_extract<double2><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+                        d_buf.as<double2>(), m.nx, m.ny, row, tcc, Bs, offs[c], t0, m.nz, c >= 4 ? 1 : 0,
+                        quad.as<double2>());
                 EGX_CUDA(cudaGetLastError());
                 if (launches) *launches += 2;
             }

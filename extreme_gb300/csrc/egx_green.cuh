@@ -32,6 +32,7 @@ struct GreenBuildStats {
 // which depend only on the lateral mesh and the radii -- not on frequency.
 struct GreenWorkspace {
     DevBuf d_lam, d_lay, d_trans, d_U, d_I, d_rho, d_gidx, d_flags, d_neg, d_radii, d_IA, d_IB, d_buf, tw0, tw1;
+    DevBuf d_buf32, tw0_32, tw1_32;  // the complex64 lateral FFT of the mixed form
     std::vector<double> key;  // nx, ny, dx, dy and the radii of the cached term lists
     DevBuf rowptr[6], terms[6];
     long nterms[6] = {};
@@ -54,9 +55,13 @@ void build_level_green(const GreenModel &m, int n_hankels, double z, double shif
                        cudaStream_t s, DevBuf &out, long *launches, GreenWorkspace &ws);
 
 // Build the spectral tensor into `quad` (device, complex128, layout of
-// GreenDims: quadrant points x [xx|xy|yy|zz|xz|yz] blocks).
+// GreenDims: quadrant points x [xx|xy|yy|zz|xz|yz] blocks). The layer
+// recursions, Hankel sums, segment and face integrals run in FP64; with
+// `lateral_fft32` (and 2nx, 2ny in {64, 128, 256, 512}) the face integrals
+// are rounded to complex64 and the 2-D lateral FFT runs in complex64, its
+// result widened into `quad`.
 void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &quad, GreenBuildStats *stats,
-                 long *launches, Timers *timers = nullptr, GreenWorkspace *ws = nullptr);
+                 long *launches, Timers *timers = nullptr, GreenWorkspace *ws = nullptr, bool lateral_fft32 = false);
 
 // Index of the background layer holding each anomaly layer; throws
 // EGX_ERR_MODEL when a layer straddles an interface (ModelUtils.cs:160-185).

@@ -505,6 +505,8 @@ void fft_lines_sym(C<T> *buf, int nlines, long lstride, long estride, int B, int
 
 template void fft_lines_sym<double>(C<double> *, int, long, long, int, int, int, int, const C<double> *, int,
                                     cudaStream_t, long *);
+template void fft_lines_sym<float>(C<float> *, int, long, long, int, int, int, int, const C<float> *, int,
+                                   cudaStream_t, long *);
 
 template void fft_lines<double>(C<double> *, int, long, long, int, int, int, const FftPlan &, const C<double> *, int,
                                 cudaStream_t, long *);

@@ -119,10 +119,14 @@ int egx_set_stream(egx_ctx *ctx, void *stream);
 long egx_launch_count(egx_ctx *ctx);
 
 /* ---- Green tensor (GreenTensor, AtoAGreenTensorCalculatorComponent) ----- */
-/* Build the anomaly-to-anomaly tensor on the device in FP64
+/* Build the anomaly-to-anomaly tensor on the device
  * (AtoAGreenTensorCalculatorComponent.CalculateGreenTensor,
- * AtoAGreenTensorCalculatorComponent.cs:69-89). precision: EGX_PREC_FP64
- * keeps complex128, EGX_PREC_MIXED also keeps a complex64 copy. */
+ * AtoAGreenTensorCalculatorComponent.cs:69-89). EGX_PREC_FP64: all in FP64,
+ * complex128 storage. EGX_PREC_MIXED: layer recursions, Hankel sums and face
+ * integrals in FP64, the 2-D lateral FFT in complex64 (when 2nx and 2ny are
+ * in {64, 128, 256, 512}; else FP64), stored as complex64 (for the inner
+ * solves) and widened to complex128 (for the refinement's residual); within
+ * ~1e-7 of the FP64 tensor. */
 int egx_green_build(egx_ctx *ctx, const egx_model *model, double omega, int n_hankels,
                     int precision, egx_green **out);
 /* Upload a spectral tensor given in the reference layout: comps[6] =

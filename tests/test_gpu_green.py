@@ -1,6 +1,7 @@
 """GPU: the FP64 anomaly-to-anomaly Green tensor built on the device against
 the oracle (per component, <= 1e-10 relative in the 2-norm) and the
-operator built from it."""
+operator built from it. The mixed form's tensor (FP64 recursions, Hankel
+sums and face integrals, complex64 lateral FFT) is within 1e-6 of it."""
 import os
 
 import numpy as np
@@ -47,6 +48,20 @@ def test_green_build_small_matches_oracle(egx_ctx, freq):
     x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
     assert rel(egx_ctx.op_apply(x), op.apply(want, om, x, op.OP_A)) < 1e-10
     g.free()
+
+
+@pytest.mark.parametrize("freq", [0.1, 10.0])
+def test_mixed_green_lateral_fft32(egx_ctx, freq):
+    m = small_model()
+    om = OmegaModel.build(m, freq)
+    g64 = egx_ctx.green_build(m, om.omega, n_hankels=10)
+    g32 = egx_ctx.green_build(m, om.omega, 10, egx.PREC_MIXED)
+    A, B = g64.download(), g32.download()
+    for c in COMPS:
+        err = rel(B[c], A[c])
+        assert 1e-12 < err < 1e-6, (c, err)   # complex64 transform: not bit-equal, within single precision
+    g64.free()
+    g32.free()
 
 
 def test_green_build_rejects_straddling_layer(egx_ctx):
