@@ -124,9 +124,12 @@ __global__ void k_bwd_y(const C<T> *__restrict__ buf, const C<T> *__restrict__ x
 // ------------------------------------------------------------------
 // The same three steps on the register-resident DFT (egx_fft_reg.cuh) for
 // lengths in {64, 128, 256, 512}: one CTA per line and 128-byte tile of
-// columns, every global access a whole 128-byte row segment.
+// columns, every global access a whole 128-byte row segment. The y passes
+// are latency-bound on their global loads: they are compiled for two CTAs
+// per SM (at 1,024 threads per CTA that is 32 registers and a few spilled
+// words, which measured faster than one CTA with 48 registers).
 template <typename T, int N>
-__global__ void __launch_bounds__(reg_threads<N, T>())
+__global__ void __launch_bounds__(reg_threads<N, T>(), 2)
     k_fwd_y_r(const C<T> *__restrict__ x, const OperatorData<T> op, C<T> *__restrict__ buf, const OpDims d,
               const C<T> *__restrict__ tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -166,7 +169,7 @@ __global__ void __launch_bounds__(reg_threads<N, T>())
 }
 
 template <typename T, int N>
-__global__ void __launch_bounds__(reg_threads<N, T>())
+__global__ void __launch_bounds__(reg_threads<N, T>(), 2)
     k_bwd_y_r(const C<T> *__restrict__ buf, const C<T> *__restrict__ x, const OperatorData<T> op,
               C<T> *__restrict__ y, const OpDims d, const C<T> *__restrict__ tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
