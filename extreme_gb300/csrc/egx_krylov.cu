@@ -53,11 +53,16 @@ __device__ double block_sum(double v) {
 
 // Each thread keeps the partial sums of up to kDotCols columns in
 // registers, so w is read once per kDotCols columns (the stacked vectors are
-// larger than L2).
+// larger than L2), and reads DotRows<T> rows per pass, so that enough loads
+// are in flight: eight rows reached 4.2-4.6 TB/s for 1-30 complex64 columns
+// where two rows reached 2.5-3.7.
 constexpr int kDotCols = 16;
+template <typename T> struct DotRows { static constexpr int value = 8; };
+template <> struct DotRows<double> { static constexpr int value = 4; };
 template <typename T>
 __global__ void k_multi_dot(const C<T> *__restrict__ V, int ncols, const C<T> *__restrict__ w, long n,
                             double2 *__restrict__ partials) {
+    constexpr int ROWS = DotRows<T>::value;
     const long stride = (long)gridDim.x * blockDim.x;
     for (int k0 = 0; k0 < ncols; k0 += kDotCols) {
         const int kc = min(kDotCols, ncols - k0);
@@ -65,19 +70,22 @@ __global__ void k_multi_dot(const C<T> *__restrict__ V, int ncols, const C<T> *_
         C<T> acc[kDotCols];
 #pragma unroll
         for (int j = 0; j < kDotCols; j++) acc[j] = mk<T>(0, 0);
-        // two rows per thread and pass: twice the loads in flight
         long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
-        for (; r + stride < n; r += 2 * stride) {
-            const C<T> x0 = w[r], x1 = w[r + stride];
+        for (; r + (ROWS - 1) * stride < n; r += ROWS * stride) {
+            C<T> x[ROWS];
+#pragma unroll
+            for (int u = 0; u < ROWS; u++) x[u] = w[r + u * stride];
 #pragma unroll
             for (int j = 0; j < kDotCols; j++)
                 if (j < kc) {
-                    const C<T> a0 = col[(long)j * n + r], a1 = col[(long)j * n + r + stride];
-                    cfma_conj<T>(acc[j], a0, x0);
-                    cfma_conj<T>(acc[j], a1, x1);
+                    C<T> a[ROWS];
+#pragma unroll
+                    for (int u = 0; u < ROWS; u++) a[u] = col[(long)j * n + r + u * stride];
+#pragma unroll
+                    for (int u = 0; u < ROWS; u++) cfma_conj<T>(acc[j], a[u], x[u]);
                 }
         }
-        if (r < n) {
+        for (; r < n; r += stride) {
             const C<T> x = w[r];
 #pragma unroll
             for (int j = 0; j < kDotCols; j++)
