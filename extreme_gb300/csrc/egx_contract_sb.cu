@@ -19,14 +19,18 @@
 // is split into a rounded high part and a remainder (three products per
 // pair: hi.hi + hi.lo + lo.hi), which keeps complex64 accuracy.
 //
-// Work split per CTA (one per SM, loop over stored points): 9 warps as
-// 3 row groups x 3 column groups; each warp owns 1/3 of the 16-row tiles and
-// 1/3 of the 8-column tiles, keeps the offsets of its A fragments in
+// Work split per CTA (one per SM, loop over stored points): 12 warps as
+// 3 row groups x 4 column groups; each warp owns 1/3 of the 16-row tiles and
+// 1/4 of the 8-column tiles, keeps the offsets of its A fragments in
 // registers (built once), and accumulates one partial product per row tile.
 // The -A^T blocks (z rows, x|y columns) are exactly the tiles of row group 2
-// and column groups 0 and 1, so their sign goes onto those warps' B
-// fragments. Column groups 1 and 2 leave partials in shared memory; group 0
-// adds them and stores.
+// and the x|y column tiles, so their sign goes onto those warps' B values.
+// The column groups' partial sums meet in shared memory, where warp w < MT
+// adds those of row tile w and stores.
+//
+// Two kernels: k_contract_sb<NZ, 1> for one right-hand side, and
+// k_contract_sb3<NZ> for two (the stacked solve of both polarisations),
+// which uses three real products per complex product (below).
 //
 // Per stored point: one TMA bulk copy of the block and one per present
 // right-hand-side segment into one of two stages, issued two points ahead
