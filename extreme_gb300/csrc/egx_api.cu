@@ -6,6 +6,7 @@
 #include <cstring>
 
 #include "egx_ctx.cuh"
+#include "egx_wait.cuh"
 
 using namespace egx;
 typedef std::complex<double> cd;
@@ -289,6 +290,20 @@ GmresResult fgmres_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_gmr
 // stacked residual below itol * sqrt(nrhs) bounds every block's by the same),
 // every apply is one nrhs-vector apply, and the refinement stops when every
 // block's own complex128 residual is below tol. true_be[i] per block.
+// Failure-detection check: a barrier that nothing completes, waited on
+// through the bounded wait of the TMA-fed kernels.
+__global__ void k_wait_probe(uint64_t limit_ns, int *err) {
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const bool done = mbar_wait_ns(b, 0, limit_ns);  // phase 0 never completes
+    if (__syncthreads_or(!done) && threadIdx.x == 0) atomicExch(err, EGX_ERR_TIMEOUT);
+}
+
 static const double kInnerSafety = 0.3;
 GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixed_params &p, int *applies,
                       int *refinements, double *true_be, int nrhs) {
@@ -773,6 +788,19 @@ int egx_mixed_solve(egx_ctx *ctx, const double *b, double *x, const egx_mixed_pa
         return fail(ctx, EGX_ERR_INVALID, e.what());
     }
     return status;
+}
+
+int egx_wait_selftest(egx_ctx *ctx, double limit_ms) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(limit_ms >= 1 && limit_ms <= 2000, EGX_ERR_INVALID, "limit_ms must be in [1, 2000]");
+        set_device(ctx);
+        k_wait_probe<<<1, 32, 0, ctx->stream>>>((uint64_t)(limit_ms * 1e6), ctx->errflag.as<int>());
+        ctx->launches++;
+        EGX_CUDA(cudaGetLastError());
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        check_device_error(ctx);  // EGX_ERR_TIMEOUT when the wait gave up; clears the flag
+    });
 }
 
 int egx_dot_products(egx_ctx *ctx, const double *V, int ncols, const double *w, long n, double *out, int where) {

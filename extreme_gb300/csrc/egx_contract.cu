@@ -25,6 +25,7 @@
 #include <cstdint>
 
 #include "egx_operator.cuh"
+#include "egx_wait.cuh"
 
 namespace egx {
 
@@ -34,35 +35,13 @@ __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ uint64_t global_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
 // Bounded wait: true when the phase completed within the limit.
-__device__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint64_t limit_ns) {
-    const uint64_t t0 = global_ns();
-    while (!mbar_try(bar, parity)) {
-        if (global_ns() - t0 > limit_ns) return false;
-    }
-    return true;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint64_t limit_ns) {
+    return mbar_wait_ns(smem_addr(bar), parity, limit_ns);
 }
 
 // One bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned)

@@ -41,6 +41,7 @@
 
 #include "egx_krylov.cuh"
 #include "egx_operator.cuh"
+#include "egx_wait.cuh"
 
 namespace egx {
 
@@ -48,29 +49,8 @@ namespace {
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ uint64_t gtime_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ bool bar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
-    const uint64_t t0 = gtime_ns();
-    while (!bar_try(bar, parity))
-        if (gtime_ns() - t0 > limit_ns) return false;
-    return true;
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
+    return mbar_wait_ns(bar, parity, limit_ns);
 }
 
 __device__ __forceinline__ void bar_expect(uint32_t bar, uint32_t bytes) {

@@ -26,7 +26,7 @@ EXPORTS = [
     "egx_op_prepare", "egx_op_apply", "egx_op_apply_c64", "egx_fft2d",
     "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products", "egx_dot_products_static",
     "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_read",
-    "egx_level_fields", "egx_level_cache", "egx_mt_responses",
+    "egx_level_fields", "egx_level_cache", "egx_mt_responses", "egx_wait_selftest",
 ]
 
 # kernel kinds of egx_profile_read
@@ -115,6 +115,7 @@ def load(path=None):
     lib.egx_level_fields.argtypes = [vp, C.POINTER(Model), d, i, d, d, d, vp, i, vp, vp, i]
     lib.egx_mt_responses.argtypes = [vp, vp, vp, vp, C.c_long, d, vp, vp, vp]
     lib.egx_level_cache.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_long)]
+    lib.egx_wait_selftest.argtypes = [vp, d]
     lib.egx_profile.argtypes = [vp, i]
     lib.egx_profile_read.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_double)]
     _lib = lib
@@ -310,6 +311,14 @@ class Context:
         if rc not in (OK, ERR_NOT_CONVERGED):
             self._check(rc)
         return jq, chi, [r.as_dict() for r in res]
+
+    def wait_selftest(self, limit_ms=100.0):
+        """egx_wait_selftest: the status code (EGX_ERR_TIMEOUT expected) and
+        the library's message."""
+        rc = self.lib.egx_wait_selftest(self.h, float(limit_ms))
+        buf = C.create_string_buffer(1024)
+        self.lib.egx_last_error(self.h, buf, 1024)
+        return rc, buf.value.decode()
 
     def level_cache(self, capacity=-1):
         """Set the level-tensor cache capacity (0..4; -1 keeps it) and return

@@ -169,6 +169,13 @@ int egx_mixed_solve(egx_ctx *ctx, const double *b, double *x, const egx_mixed_pa
  * z_j = M(v_j) of the outer FGMRES to fn(user, ...). */
 int egx_set_precond(egx_ctx *ctx, int kind, egx_precond_fn fn, void *user);
 
+/* Failure-detection check (no reference counterpart): one kernel waits,
+ * through the bounded wait that every TMA-fed kernel uses, on a shared-memory
+ * barrier that nothing completes, and gives up after limit_ms (1..2000).
+ * Returns EGX_ERR_TIMEOUT (message from egx_last_error) with the context
+ * still usable; EGX_OK would mean that the wait did not give up. */
+int egx_wait_selftest(egx_ctx *ctx, double limit_ms);
+
 /* DotProductRequest (AnomalyCurrentFgmresSolver.cs:115-130): out[k] =
  * conj(V[:, k])^T w for k < ncols, V column-major with leading dimension n. */
 int egx_dot_products(egx_ctx *ctx, const double *V, int ncols, const double *w, long n, double *out, int where);
