@@ -6,6 +6,7 @@
 #include <cstring>
 
 #include "egx_ctx.cuh"
+#include "egx_learn.cuh"
 #include "egx_wait.cuh"
 
 using namespace egx;
@@ -105,6 +106,10 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
         outer = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->outer64);
         inner = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->inner64);
         key = &ctx->key64;
+    } else if (precond_kind == EGX_PRECOND_LEARNED) {
+        outer = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->outer32l);
+        inner = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->inner32l);
+        key = &ctx->key32l;
     } else {
         outer = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->outer32);
         inner = reinterpret_cast<std::unique_ptr<Gmres<T>> *>(&ctx->inner32);
@@ -116,7 +121,8 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
         outer->reset();
         inner->reset();
         outer->reset(new Gmres<T>(n, m_out, tol, max_restarts, check_true, ctx->stream));
-        if (precond_kind == EGX_PRECOND_GMRES) inner->reset(new Gmres<T>(n, m_in, tol, 1, false, ctx->stream));
+        if (precond_kind == EGX_PRECOND_GMRES || precond_kind == EGX_PRECOND_LEARNED)
+            inner->reset(new Gmres<T>(n, m_in, tol, 1, false, ctx->stream));
         *key = keybuf;
     }
     // the inner GMRES runs one cycle to the outer tolerance
@@ -135,6 +141,20 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
         (*inner)->timers = &ctx->timers;
         Gmres<T> *in = inner->get();
         (*outer)->precond = [in](const C<T> *src, C<T> *dst) { in->solve(src, src, dst); };
+    } else if (precond_kind == EGX_PRECOND_LEARNED) {
+        EGX_CHECK(!dbl && ctx->precond_user, EGX_ERR_STATE, "learned preconditioner without a network");
+        // the network's estimate of A^-1 v starts the inner GMRES cycle in
+        // place of v itself (x0 = v in FlexibleGmresWithGmresPreconditioner.cs:35-44)
+        egx_net *net = static_cast<egx_net *>(ctx->precond_user);
+        EGX_CHECK(net_length(net) == nvec(ctx), EGX_ERR_INVALID, "learned preconditioner built for another grid");
+        (*inner)->apply = apply;
+        (*inner)->timers = &ctx->timers;
+        Gmres<T> *in = inner->get();
+        (*outer)->precond = [ctx, net, nrhs, in](const C<T> *src, C<T> *dst) {
+            net_apply(net, reinterpret_cast<const float2 *>(src), reinterpret_cast<float2 *>(dst), nrhs, ctx->stream,
+                      &ctx->launches);
+            in->solve(src, dst, dst);
+        };
     } else if (precond_kind == EGX_PRECOND_CALLBACK) {
         egx_precond_fn fn = ctx->precond_fn;
         void *user = ctx->precond_user;
@@ -377,8 +397,28 @@ GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixe
         // ask the inner solve only for the reduction still needed (with a
         // safety factor), never for less than inner_tol
         double itol = std::max(p.inner_tol, std::min(0.5, kInnerSafety * p.tol / bemax)) / std::sqrt((double)nrhs);
-        GmresResult ir = run_fgmres<float>(ctx, r32, d32, p.m_out, p.m_in, itol, p.inner_restarts, false,
-                                           EGX_PRECOND_GMRES, &a32, nrhs);
+        GmresResult ir;
+        bool done = false;
+        if (ctx->precond_kind == EGX_PRECOND_LEARNED) {
+            // the network as the flexible preconditioner, with the inner
+            // solve's restart budget; then the GMRES-preconditioned solve
+            // from zero (the fallback)
+            ctx->learned_uses++;
+            ir = run_fgmres<float>(ctx, r32, d32, p.m_out, p.m_in, itol, p.inner_restarts, false,
+                                   EGX_PRECOND_LEARNED, &a32, nrhs);
+            done = ir.converged;
+            if (!done) {
+                ctx->learned_fallbacks++;
+                applies32 += a32;
+                out.iterations += ir.iterations;
+                VecOps<float>::zero(d32, N, ctx->stream);
+                ctx->launches++;
+            }
+        }
+        if (!done)
+            ir = run_fgmres<float>(ctx, r32, d32, p.m_out, p.m_in, itol, p.inner_restarts, false,
+                                   ctx->precond_kind == EGX_PRECOND_NONE ? EGX_PRECOND_NONE : EGX_PRECOND_GMRES, &a32,
+                                   nrhs);
         applies32 += a32;
         out.iterations += ir.iterations;
         out.arnoldi_be = ir.arnoldi_be;
@@ -400,16 +440,6 @@ GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixe
 }
 
 }  // namespace egx
-
-#define EGX_GUARD(ctx, ...)                                             \
-    try {                                                               \
-        __VA_ARGS__;                                                    \
-        return EGX_OK;                                                  \
-    } catch (const egx::Error &e) {                                     \
-        return fail((ctx), e.code, e.what());                           \
-    } catch (const std::exception &e) {                                 \
-        return fail((ctx), EGX_ERR_INVALID, e.what());                  \
-    }
 
 extern "C" {
 
@@ -696,9 +726,11 @@ int egx_fft2d(egx_ctx *ctx, double *buf, int n0, int n1, int howmany, int sign, 
 
 int egx_set_precond(egx_ctx *ctx, int kind, egx_precond_fn fn, void *user) {
     if (!ctx) return EGX_ERR_INVALID;
-    if (kind != EGX_PRECOND_GMRES && kind != EGX_PRECOND_CALLBACK && kind != EGX_PRECOND_NONE)
+    if (kind != EGX_PRECOND_GMRES && kind != EGX_PRECOND_CALLBACK && kind != EGX_PRECOND_NONE &&
+        kind != EGX_PRECOND_LEARNED)
         return fail(ctx, EGX_ERR_INVALID, "unknown preconditioner kind");
     if (kind == EGX_PRECOND_CALLBACK && !fn) return fail(ctx, EGX_ERR_INVALID, "callback preconditioner without fn");
+    if (kind == EGX_PRECOND_LEARNED && !user) return fail(ctx, EGX_ERR_INVALID, "learned preconditioner without net");
     ctx->precond_kind = kind;
     ctx->precond_fn = fn;
     ctx->precond_user = user;
@@ -788,6 +820,13 @@ int egx_mixed_solve(egx_ctx *ctx, const double *b, double *x, const egx_mixed_pa
         return fail(ctx, EGX_ERR_INVALID, e.what());
     }
     return status;
+}
+
+int egx_learned_stats(egx_ctx *ctx, long *uses, long *fallbacks) {
+    if (!ctx) return EGX_ERR_INVALID;
+    if (uses) *uses = ctx->learned_uses;
+    if (fallbacks) *fallbacks = ctx->learned_fallbacks;
+    return EGX_OK;
 }
 
 int egx_wait_selftest(egx_ctx *ctx, double limit_ms) {

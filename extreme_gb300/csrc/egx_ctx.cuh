@@ -47,6 +47,10 @@ struct egx_ctx {
     std::unique_ptr<egx::Gmres<double>> outer64, inner64;
     std::unique_ptr<egx::Gmres<float>> outer32, inner32;
     std::string key64, key32;
+    // inner solves with the learned preconditioner keep their own workspace
+    std::unique_ptr<egx::Gmres<float>> outer32l, inner32l;
+    std::string key32l;
+    long learned_uses = 0, learned_fallbacks = 0;
     // preconditioner plug
     int precond_kind = EGX_PRECOND_GMRES;
     egx_precond_fn precond_fn = nullptr;
@@ -72,6 +76,18 @@ struct egx_ctx {
     unsigned long long lvl_clock = 0;
     long lvl_hits = 0, lvl_builds = 0;
 };
+
+// Body of a C entry point: returns EGX_OK, or the status of the exception
+// with its message kept for egx_last_error (exceptions never cross the ABI).
+#define EGX_GUARD(ctx, ...)                                             \
+    try {                                                               \
+        __VA_ARGS__;                                                    \
+        return EGX_OK;                                                  \
+    } catch (const egx::Error &e) {                                     \
+        return fail((ctx), e.code, e.what());                           \
+    } catch (const std::exception &e) {                                 \
+        return fail((ctx), EGX_ERR_INVALID, e.what());                  \
+    }
 
 namespace egx {
 

@@ -454,7 +454,7 @@ GmresResult Gmres<T>::solve(const C<T> *rhs, const C<T> *x0, C<T> *result) {
     kernel_launches += 1;
     double beta = norm(w_);
     if (beta == 0) {
-        VecOps<T>::copy(x0, result, n_, s_);
+        if (x0 != result) VecOps<T>::copy(x0, result, n_, s_);
         res.converged = true;
         res.arnoldi_be = 0;
         res.true_be = 0;
@@ -463,7 +463,7 @@ GmresResult Gmres<T>::solve(const C<T> *rhs, const C<T> *x0, C<T> *result) {
     }
     double bea = -1, be = -1;
     int iter = 0;
-    VecOps<T>::copy(x0, result, n_, s_);
+    if (x0 != result) VecOps<T>::copy(x0, result, n_, s_);
     while (true) {
         VecOps<T>::scale(w_, 1.0 / beta, V_, n_, s_);
         kernel_launches += 1;

@@ -17,7 +17,7 @@ ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_NOT_CONVERGED, ERR_TIMEOUT, ERR_STATE, ERR_M
 OP_A, OP_CHI0 = 0, 1
 HOST, DEVICE = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
-PRECOND_GMRES, PRECOND_CALLBACK, PRECOND_NONE = 0, 1, 2
+PRECOND_GMRES, PRECOND_CALLBACK, PRECOND_NONE, PRECOND_LEARNED = 0, 1, 2, 3
 
 # Every symbol the header declares (checked by the ABI test).
 EXPORTS = [
@@ -27,6 +27,8 @@ EXPORTS = [
     "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products", "egx_dot_products_static",
     "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_read",
     "egx_level_fields", "egx_level_cache", "egx_mt_responses", "egx_wait_selftest",
+    "egx_net_create", "egx_net_free", "egx_net_size", "egx_net_params", "egx_net_set_model", "egx_net_loss_grad",
+    "egx_net_adam", "egx_net_apply", "egx_learned_stats",
 ]
 
 # kernel kinds of egx_profile_read
@@ -116,6 +118,16 @@ def load(path=None):
     lib.egx_mt_responses.argtypes = [vp, vp, vp, vp, C.c_long, d, vp, vp, vp]
     lib.egx_level_cache.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_long)]
     lib.egx_wait_selftest.argtypes = [vp, d]
+    lib.egx_net_create.argtypes = [vp, i, i, i, i, i, C.c_uint, C.POINTER(vp)]
+    lib.egx_net_free.argtypes = [vp, vp]
+    lib.egx_net_size.argtypes = [vp]
+    lib.egx_net_size.restype = C.c_long
+    lib.egx_net_params.argtypes = [vp, vp, vp, i]
+    lib.egx_net_set_model.argtypes = [vp, vp, vp]
+    lib.egx_net_loss_grad.argtypes = [vp, vp, vp, vp, i, C.POINTER(C.c_float), vp, i]
+    lib.egx_net_adam.argtypes = [vp, vp, C.c_float]
+    lib.egx_net_apply.argtypes = [vp, vp, vp, vp, i, i]
+    lib.egx_learned_stats.argtypes = [vp, C.POINTER(C.c_long), C.POINTER(C.c_long)]
     lib.egx_profile.argtypes = [vp, i]
     lib.egx_profile_read.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_double)]
     _lib = lib
@@ -356,6 +368,20 @@ class Context:
         self._check(self.lib.egx_profile_read(self.h, kind, C.byref(n), C.byref(ms)))
         return n.value, ms.value
 
+    def set_learned(self, net):
+        """Mixed inner solves whose preconditioner is the inner GMRES cycle
+        started from the network's estimate of A^-1 v (GMRES from v as the
+        fallback); net=None goes back to the GMRES preconditioner."""
+        if net is None:
+            self.set_precond(PRECOND_GMRES)
+        else:
+            self._check(self.lib.egx_set_precond(self.h, PRECOND_LEARNED, PRECOND_FN(), net.h))
+
+    def learned_stats(self):
+        uses, fb = C.c_long(), C.c_long()
+        self._check(self.lib.egx_learned_stats(self.h, C.byref(uses), C.byref(fb)))
+        return uses.value, fb.value
+
     def set_precond(self, kind, fn=None):
         """fn(src_ptr, dst_ptr, n, precision) -> None, device pointers."""
         if kind == PRECOND_CALLBACK:
@@ -370,6 +396,75 @@ class Context:
         else:
             self._cb = None
             self._check(self.lib.egx_set_precond(self.h, kind, PRECOND_FN(), None))
+
+
+class SpectralNet:
+    """The learned preconditioner's network (egx_net_*): z = v + rms(v) N(v/rms(v))
+    for complex64 vectors in the anomaly layout, batches [B, N]."""
+
+    def __init__(self, ctx, nx, ny, nz, width=32, layers=4, seed=0):
+        self.ctx, self.nx, self.ny, self.nz = ctx, nx, ny, nz
+        h = C.c_void_p()
+        ctx._check(ctx.lib.egx_net_create(ctx.h, nx, ny, nz, width, layers, seed, C.byref(h)))
+        self.h = h
+        self.n = nx * ny * 3 * nz
+
+    @property
+    def size(self):
+        return self.ctx.lib.egx_net_size(self.h)
+
+    def params(self, values=None):
+        """Read (values None) or write the flat FP32 parameter vector."""
+        if values is None:
+            out = np.empty(self.size, np.float32)
+            self.ctx._check(self.ctx.lib.egx_net_params(self.ctx.h, self.h, _ptr(out), 0))
+            return out
+        v = np.ascontiguousarray(values, np.float32)
+        assert v.size == self.size
+        self.ctx._check(self.ctx.lib.egx_net_params(self.ctx.h, self.h, _ptr(v), 1))
+
+    def set_model(self, logsig):
+        """log10(omega mu0 sigma dx dy) per anomaly cell, [nx, ny, nz]."""
+        ls = np.ascontiguousarray(logsig, np.float32)
+        assert ls.shape == (self.nx, self.ny, self.nz)
+        self.ctx._check(self.ctx.lib.egx_net_set_model(self.ctx.h, self.h, _ptr(ls)))
+
+    def loss_grad(self, v, t, want_grad=False):
+        """Loss (and the flat gradient) for residuals v and target corrections
+        t = z* - v, host complex arrays [B, N]."""
+        v = np.ascontiguousarray(v, np.complex64).reshape(-1, self.n)
+        t = np.ascontiguousarray(t, np.complex64).reshape(-1, self.n)
+        loss = C.c_float()
+        g = np.empty(self.size, np.float32) if want_grad else None
+        self.ctx._check(self.ctx.lib.egx_net_loss_grad(self.ctx.h, self.h, _ptr(v), _ptr(t), v.shape[0],
+                                                       C.byref(loss), _ptr(g) if g is not None else None, HOST))
+        return (loss.value, g) if want_grad else loss.value
+
+    def loss_grad_dev(self, v_ptr, t_ptr, batch):
+        loss = C.c_float()
+        self.ctx._check(self.ctx.lib.egx_net_loss_grad(self.ctx.h, self.h, C.c_void_p(v_ptr), C.c_void_p(t_ptr),
+                                                       batch, C.byref(loss), None, DEVICE))
+        return loss.value
+
+    def adam(self, lr):
+        self.ctx._check(self.ctx.lib.egx_net_adam(self.ctx.h, self.h, float(lr)))
+
+    def apply(self, v):
+        v = np.ascontiguousarray(v, np.complex64).reshape(-1, self.n)
+        z = np.empty_like(v)
+        self.ctx._check(self.ctx.lib.egx_net_apply(self.ctx.h, self.h, _ptr(v), _ptr(z), v.shape[0], HOST))
+        return z
+
+    def free(self):
+        if self.h is not None and self.ctx.h is not None:
+            self.ctx.lib.egx_net_free(self.ctx.h, self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 class GreenTensor:

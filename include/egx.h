@@ -46,11 +46,12 @@ typedef enum {
 enum { EGX_OP_A = 0, EGX_OP_CHI0 = 1 };             /* OperatorType.cs */
 enum { EGX_HOST = 0, EGX_DEVICE = 1 };              /* where the vectors live */
 enum { EGX_PREC_FP64 = 0, EGX_PREC_MIXED = 1 };     /* storage/arithmetic of the operator */
-enum { EGX_PRECOND_GMRES = 0, EGX_PRECOND_CALLBACK = 1, EGX_PRECOND_NONE = 2 };
+enum { EGX_PRECOND_GMRES = 0, EGX_PRECOND_CALLBACK = 1, EGX_PRECOND_NONE = 2, EGX_PRECOND_LEARNED = 3 };
 enum { EGX_FFT_FORWARD = -1, EGX_FFT_BACKWARD = 1 }; /* FFTW sign convention */
 
 typedef struct egx_ctx egx_ctx;
 typedef struct egx_green egx_green;
+typedef struct egx_net egx_net;
 
 /* Cartesian model at one frequency's geometry (CartesianModel, Section1D). */
 typedef struct {
@@ -168,6 +169,41 @@ int egx_mixed_solve(egx_ctx *ctx, const double *b, double *x, const egx_mixed_pa
 /* RightPreconditionerRequest plug point: kind EGX_PRECOND_CALLBACK routes
  * z_j = M(v_j) of the outer FGMRES to fn(user, ...). */
 int egx_set_precond(egx_ctx *ctx, int kind, egx_precond_fn fn, void *user);
+
+/* ---- learned flexible preconditioner (the RightPreconditionerRequest plug
+ * point, FlexibleGmresSolver.cs:24-36; no reference counterpart otherwise) --
+ * A spectral network on the lateral grid proposes the correction z - v,
+ * z ~ A^-1 v, from the residual v and the log-conductivity:
+ * z = v + rms(v) N(v / rms(v)). Input per lateral cell: Re, Im of the three
+ * residual components and log10(omega mu0 sigma dx dy) of every anomaly
+ * layer; `layers` spectral layers of `width` channels, 16 x 16 lateral modes
+ * (real Fourier basis), GELU; BF16 tensor-core GEMMs with FP32 accumulation
+ * for the forward and backward passes, Adam. Vectors are complex64 [batch][N]
+ * in the anomaly layout; batch <= 64. The output layer starts at zero: an
+ * untrained network is the identity. */
+int egx_net_create(egx_ctx *ctx, int nx, int ny, int nz, int width, int layers, unsigned seed, egx_net **out);
+int egx_net_free(egx_ctx *ctx, egx_net *net);
+long egx_net_size(const egx_net *net);                               /* parameters */
+int egx_net_params(egx_ctx *ctx, egx_net *net, float *host, int set);  /* set = 0 read, 1 write */
+/* log-conductivity channel, [nx][ny][nz] host floats */
+int egx_net_set_model(egx_ctx *ctx, egx_net *net, const float *logsig);
+/* loss = mean_b |N(v_b/rms_b) - t_b/rms_b|^2 / |t_b/rms_b|^2 for targets t = z* - v;
+ * gradients kept for egx_net_adam and copied to grad (n_params floats) if not NULL */
+int egx_net_loss_grad(egx_ctx *ctx, egx_net *net, const float *v, const float *t, int batch, float *loss, float *grad,
+                      int where);
+int egx_net_adam(egx_ctx *ctx, egx_net *net, float lr);
+int egx_net_apply(egx_ctx *ctx, egx_net *net, const float *v, float *z, int batch, int where);
+/* With egx_set_precond(ctx, EGX_PRECOND_LEARNED, NULL, net) the inner solves
+ * of the mixed form are FGMRES whose flexible preconditioner is the
+ * reference's inner GMRES(m_in) cycle started from the network's estimate
+ * v + rms(v) N(v/rms(v)) of A^-1 v instead of from v
+ * (FlexibleGmresWithGmresPreconditioner.cs:35-44); the network must be built
+ * for the solve's grid (EGX_ERR_INVALID otherwise). An inner solve that does
+ * not reach its tolerance is redone with the GMRES preconditioner (the
+ * fallback), and the refinement's complex128 residual judges the result.
+ * uses/fallbacks count the inner solves since the context was created.
+ * EGX_PRECOND_NONE makes the mixed form's inner FGMRES unpreconditioned. */
+int egx_learned_stats(egx_ctx *ctx, long *uses, long *fallbacks);
 
 /* Failure-detection check (no reference counterpart): one kernel waits,
  * through the bounded wait that every TMA-fed kernel uses, on a shared-memory

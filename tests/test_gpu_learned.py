@@ -1,0 +1,185 @@
+"""GPU: the learned preconditioner's network (egx_net_*) against the numpy
+oracle -- forward, loss and every parameter block of the gradient (BF16
+tensor-core GEMMs with FP32 accumulation against FP64) -- the identity of an
+untrained network, Adam lowering the loss, and the mixed solve with the
+network as its flexible preconditioner reaching the 1e-6 target."""
+import numpy as np
+import pytest
+
+from oracle import spectral_net as sn
+
+pytestmark = pytest.mark.gpu
+
+# BF16 operands (8-bit significand), FP32 accumulation: normwise relative
+# error per parameter block against the FP64 oracle
+GRAD_TOL = 5e-2
+LOSS_TOL = 2e-2
+APPLY_TOL = 3e-2
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from extreme_gb300 import egx
+    c = egx.Context(0)
+    yield c
+    c.close()
+
+
+def _net(ctx, nx, ny, nz, W, L, seed):
+    from extreme_gb300 import egx
+    net = egx.SpectralNet(ctx, nx, ny, nz, width=W, layers=L, seed=seed)
+    rng = np.random.default_rng(seed)
+    flat = net.params()
+    lay, size = sn.layout(nz, W, L)
+    assert size == net.size
+    # nonzero output layer and biases, so that every block carries gradient
+    for name in ("Q", "bQ", "bP") + tuple("b%d" % l for l in range(L)):
+        off, shape = lay[name]
+        k = int(np.prod(shape))
+        flat[off:off + k] = 0.2 * rng.standard_normal(k)
+    net.params(flat)
+    return net, flat.astype(np.float64), lay
+
+
+def _inputs(nx, ny, nz, B, seed):
+    rng = np.random.default_rng(seed + 100)
+    n = nx * ny * 3 * nz
+    v = (rng.standard_normal((B, n)) + 1j * rng.standard_normal((B, n))).astype(np.complex64)
+    t = (0.3 * (rng.standard_normal((B, n)) + 1j * rng.standard_normal((B, n)))).astype(np.complex64)
+    logsig = rng.uniform(-3, 1, (nx, ny, nz)).astype(np.float32)
+    return v, t, logsig
+
+
+@pytest.mark.parametrize("nx,ny,nz,W,L,B", [(12, 10, 2, 16, 2, 2), (32, 24, 4, 32, 3, 3)])
+def test_loss_and_gradient_match_oracle(ctx, nx, ny, nz, W, L, B):
+    net, flat, lay = _net(ctx, nx, ny, nz, W, L, seed=nx)
+    try:
+        v, t, logsig = _inputs(nx, ny, nz, B, seed=nx)
+        net.set_model(logsig)
+        loss, g = net.loss_grad(v, t, want_grad=True)
+        ref_loss, ref_g = sn.loss_grad(flat, v.astype(np.complex128), t.astype(np.complex128),
+                                       logsig.astype(np.float64), nx, ny, nz, W, L)
+        assert abs(loss - ref_loss) <= LOSS_TOL * ref_loss, (loss, ref_loss)
+        for name, (off, shape) in lay.items():
+            k = int(np.prod(shape))
+            a, b = g[off:off + k].astype(np.float64), ref_g[off:off + k]
+            err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+            assert err <= GRAD_TOL, (name, err)
+    finally:
+        net.free()
+
+
+def test_apply_matches_oracle(ctx):
+    nx, ny, nz, W, L, B = 20, 16, 3, 16, 2, 2
+    net, flat, _ = _net(ctx, nx, ny, nz, W, L, seed=5)
+    try:
+        v, _, logsig = _inputs(nx, ny, nz, B, seed=5)
+        net.set_model(logsig)
+        z = net.apply(v)
+        ref = sn.apply(flat, v.astype(np.complex128), logsig.astype(np.float64), nx, ny, nz, W, L)
+        err = np.linalg.norm(z - ref) / np.linalg.norm(ref - v)
+        assert err <= APPLY_TOL, err
+    finally:
+        net.free()
+
+
+def test_untrained_network_is_identity(ctx):
+    from extreme_gb300 import egx
+    nx, ny, nz = 16, 16, 2
+    net = egx.SpectralNet(ctx, nx, ny, nz, width=16, layers=2, seed=1)
+    try:
+        v, _, logsig = _inputs(nx, ny, nz, 2, seed=1)
+        net.set_model(logsig)
+        np.testing.assert_array_equal(net.apply(v), v)
+    finally:
+        net.free()
+
+
+def test_adam_lowers_the_loss(ctx):
+    """A learnable target (a fixed lateral smoothing of v, scaled per layer):
+    60 Adam steps on one batch lower the loss well below its start."""
+    from extreme_gb300 import egx
+    nx, ny, nz, B = 16, 16, 2, 4
+    net = egx.SpectralNet(ctx, nx, ny, nz, width=16, layers=2, seed=3)
+    try:
+        v, _, logsig = _inputs(nx, ny, nz, B, seed=3)
+        vv = v.reshape(B, nx, ny, 3, nz)
+        t = 0.5 * (vv + np.roll(vv, 1, 1) + np.roll(vv, 1, 2)) / 3.0
+        t = t.reshape(B, -1).astype(np.complex64)
+        net.set_model(logsig)
+        first = net.loss_grad(v, t)
+        for _ in range(60):
+            net.loss_grad(v, t)
+            net.adam(3e-3)
+        last = net.loss_grad(v, t)
+        assert first > 0.9 and last < 0.5 * first, (first, last)
+    finally:
+        net.free()
+
+
+def test_net_arguments_are_checked(ctx):
+    from extreme_gb300 import egx
+    with pytest.raises(egx.EgxError):
+        egx.SpectralNet(ctx, 1, 8, 2)
+    net = egx.SpectralNet(ctx, 8, 8, 2, width=8, layers=1)
+    try:
+        v = np.zeros((1, net.n), np.complex64)
+        with pytest.raises(egx.EgxError):   # no model set yet
+            net.apply(v)
+        net.set_model(np.zeros((8, 8, 2), np.float32))
+        with pytest.raises(egx.EgxError):
+            net.apply(np.zeros((65, net.n), np.complex64))
+        np.testing.assert_array_equal(net.apply(v), v)  # zero vector: rms 0, z = v
+    finally:
+        net.free()
+
+
+def test_mixed_solve_with_learned_preconditioner(ctx):
+    """Pairs from the solver on one model, a short training run, then the
+    three inner preconditioners on a held-out model. The network's estimate
+    only seeds the reference's inner GMRES cycle, so the learned solve keeps
+    the default method's apply count per outer iteration and reaches the 1e-6
+    target; the iteration counts of the three are printed (what the network
+    gains or loses)."""
+    from extreme_gb300 import egx, learned
+    from extreme_gb300.forward import MixedSettings
+    from extreme_gb300.model import scaled_model
+    nx, ny, nz = 24, 24, 4
+    f = 1.0
+    sets = [learned.collect_pairs(ctx, scaled_model(nx, ny, nz, seed=11), f, n_vectors=6)]
+    assert sets[0].v.shape == (12, nx * ny * 3 * nz)
+    held = [learned.collect_pairs(ctx, scaled_model(nx, ny, nz, seed=12), f, n_vectors=6)]
+    net = egx.SpectralNet(ctx, nx, ny, nz, width=16, layers=2, seed=0)
+    try:
+        before = learned.mean_loss(net, sets)
+        log = learned.train(net, sets, steps=60, batch=4, lr=1e-3)
+        assert np.isfinite(log.losses).all()
+        assert learned.mean_loss(net, sets) < before
+        rows = learned.evaluate(ctx, net, scaled_model(nx, ny, nz, seed=12), f, MixedSettings(tol=1e-6))
+        by = {r.method: r for r in rows}
+        for m in ("gmres", "learned"):
+            assert max(by[m].true_be) < 1e-6, (m, by[m].true_be)
+        assert by["learned"].learned_uses >= 1 and by["learned"].fallbacks == 0
+        assert by["gmres"].learned_uses == 0
+        print("held-out loss %.3f; outer iterations gmres %d none %d learned %d" % (
+            learned.mean_loss(net, held), by["gmres"].iterations[0], by["none"].iterations[0],
+            by["learned"].iterations[0]))
+    finally:
+        net.free()
+
+
+def test_learned_net_must_match_the_grid(ctx):
+    from extreme_gb300 import egx
+    from extreme_gb300.forward import MixedSettings, Mt3DForwardSolver
+    from extreme_gb300.model import scaled_model
+    m = scaled_model(16, 16, 2, seed=3)
+    net = egx.SpectralNet(ctx, 16, 12, 2, width=8, layers=1)
+    try:
+        net.set_model(np.zeros((16, 12, 2), np.float32))
+        ctx.set_learned(net)
+        solver = Mt3DForwardSolver(precision=egx.PREC_MIXED, mixed=MixedSettings(tol=1e-6), ctx=ctx)
+        with pytest.raises(egx.EgxError):
+            solver.solve(m, 1.0)
+    finally:
+        ctx.set_learned(None)
+        net.free()
