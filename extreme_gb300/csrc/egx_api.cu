@@ -262,9 +262,10 @@ void prepare_device(egx_ctx *ctx, egx_green *g, const double *dz, int type) {
 }
 
 template <typename T>
-void apply_dev(egx_ctx *ctx, const C<T> *x, C<T> *y, int nrhs) {
+void apply_dev(egx_ctx *ctx, const C<T> *x, C<T> *y, int nrhs, bool ds) {
     EGX_CHECK(ctx->g && ctx->type >= 0, EGX_ERR_STATE, "operator is not prepared (PrepareOperator not called)");
     OpDims d{ctx->nx, ctx->ny, ctx->nz, nrhs, nrhs * 3 * ctx->nz, nvec(ctx)};
+    d.ds = ds ? 1 : 0;
     size_t bufbytes = (size_t)4 * ctx->nx * ctx->ny * d.B * sizeof(C<T>);
     const bool dbl = sizeof(T) == sizeof(double);
     DevBuf &buf = dbl ? ctx->buf64 : ctx->buf32;
@@ -287,8 +288,8 @@ void apply_dev(egx_ctx *ctx, const C<T> *x, C<T> *y, int nrhs) {
     operator_apply<T>(d, op, G, x, y, buf.as<C<T>>(), tw0, tw1, ctx->p0, ctx->p1, ctx->stream, &ctx->launches,
                       &ctx->timers, ctx->errflag.as<int>());
 }
-template void apply_dev<double>(egx_ctx *, const C<double> *, C<double> *, int);
-template void apply_dev<float>(egx_ctx *, const C<float> *, C<float> *, int);
+template void apply_dev<double>(egx_ctx *, const C<double> *, C<double> *, int, bool);
+template void apply_dev<float>(egx_ctx *, const C<float> *, C<float> *, int, bool);
 
 GmresResult fgmres_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_gmres_params &p, int *applies) {
     EGX_CHECK(p.m_out >= 1 && p.m_in >= 1 && p.max_restarts >= 1 && p.tol > 0, EGX_ERR_INVALID,
@@ -381,7 +382,7 @@ GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixe
         EGX_CUDA(cudaMemcpyAsync(r, b, N * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
         bemax = residuals(r);
     } else {
-        apply_dev<double>(ctx, x, t, nrhs);
+        apply_dev<double>(ctx, x, t, nrhs, true);
         applies64++;
         VecOps<double>::sub(b, t, r, N, ctx->stream);
         ctx->launches++;
@@ -423,7 +424,7 @@ GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixe
         out.iterations += ir.iterations;
         out.arnoldi_be = ir.arnoldi_be;
         for (int i = 0; i < nrhs; i++) convert_f2d_add(d32 + i * n, x + i * n, n, rn[i], ctx->stream);
-        apply_dev<double>(ctx, x, t, nrhs);
+        apply_dev<double>(ctx, x, t, nrhs, true);
         applies64++;
         VecOps<double>::sub(b, t, r, N, ctx->stream);
         ctx->launches += 1 + nrhs;
@@ -669,6 +670,27 @@ int egx_op_apply(egx_ctx *ctx, const double *x, double *y, int nrhs, int where) 
             ctx->yout.ensure(n * sizeof(double2));
             EGX_CUDA(cudaMemcpyAsync(ctx->xin.p, x, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
             apply_dev<double>(ctx, ctx->xin.as<double2>(), ctx->yout.as<double2>(), nrhs);
+            EGX_CUDA(cudaMemcpyAsync(y, ctx->yout.p, n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        check_device_error(ctx);
+    });
+}
+
+int egx_op_apply_ds(egx_ctx *ctx, const double *x, double *y, int nrhs, int where) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(x && y && nrhs >= 1, EGX_ERR_INVALID, "bad apply arguments");
+        set_device(ctx);
+        EGX_CHECK(ctx->g, EGX_ERR_STATE, "operator is not prepared");
+        long n = nvec(ctx) * nrhs;
+        if (where == EGX_DEVICE) {
+            apply_dev<double>(ctx, (const double2 *)x, (double2 *)y, nrhs, true);
+        } else {
+            ctx->xin.ensure(n * sizeof(double2));
+            ctx->yout.ensure(n * sizeof(double2));
+            EGX_CUDA(cudaMemcpyAsync(ctx->xin.p, x, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+            apply_dev<double>(ctx, ctx->xin.as<double2>(), ctx->yout.as<double2>(), nrhs, true);
             EGX_CUDA(cudaMemcpyAsync(y, ctx->yout.p, n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
         }
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));

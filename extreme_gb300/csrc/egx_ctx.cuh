@@ -98,7 +98,9 @@ long nvec(const egx_ctx *ctx);
 void prepare_device(egx_ctx *ctx, egx_green *g, const double *dz_host, int type);
 // Upload zeta [nx][ny][nz] and zeta0 [nz] (host or device pointers).
 void upload_model(egx_ctx *ctx, egx_green *g, const double *zeta, const double *zeta0, int where);
-template <typename T> void apply_dev(egx_ctx *ctx, const C<T> *x, C<T> *y, int nrhs);
+// ds: a complex128 apply whose block contraction runs in double-FP32
+// arithmetic (the mixed form's refinement residual)
+template <typename T> void apply_dev(egx_ctx *ctx, const C<T> *x, C<T> *y, int nrhs, bool ds = false);
 GmresResult fgmres_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_gmres_params &p, int *applies);
 GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixed_params &p, int *applies,
                       int *refinements, double *true_be, int nrhs = 1);

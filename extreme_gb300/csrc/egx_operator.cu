@@ -340,6 +340,162 @@ __global__ void k_contract(C<T> *buf, const C<T> *__restrict__ G, const OpDims d
     }
 }
 
+// ---------------------------------------------------------------------------
+// The complex128 contraction in double-FP32 arithmetic (the mixed form's
+// refinement residual). GB300 runs complex128 FMAs at 1/64 of the FP32 rate,
+// which makes the FP64 block product above compute-bound; here every
+// operand is a pair of floats hi + lo (47 significant bits) and every dot
+// product runs as Dot2 (Ogita, Rump and Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26 (2005), Algorithm 5.3): each product
+// made error-free with one FMA (TwoProduct), each sum with Knuth's TwoSum,
+// the errors added in a second float. The result is as accurate as if it
+// had been computed in ~47-bit arithmetic and then rounded to complex128.
+
+// v = h + l: h keeps the sign, the exponent and the top 23 stored mantissa
+// bits of v, l the next 23 bits; built from the bit pattern with integer
+// and FP32 operations only (no complex128 conversion in the hot loop).
+// |v| < 2^-80 keeps only h; |v| < 2^-126 flushes to zero.
+__device__ __forceinline__ void ds_split(double v, float &h, float &l) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const unsigned w1 = (unsigned)(u >> 32), w0 = (unsigned)u;
+    const unsigned sgn = w1 & 0x80000000u;
+    const int e = (int)((w1 >> 20) & 0x7FFu);
+    const int eh = e - 896;  // biased float exponent of h
+    const unsigned mh = ((w1 & 0xFFFFFu) << 3) | (w0 >> 29);
+    h = (eh >= 1 && eh <= 254) ? __int_as_float((int)(sgn | ((unsigned)eh << 23) | mh)) : 0.f;
+    const unsigned r = (w0 & 0x1FFFFFFFu) >> 6;                                     // 23 bits
+    const float fr = __fsub_rn(__int_as_float((int)(0x4B000000u | r)), 8388608.f);  // exactly r
+    const int el = e - 942;  // biased float exponent of 2^(e - 1023 - 46)
+    const float sc = (el >= 1 && el <= 254) ? __int_as_float(el << 23) : 0.f;
+    l = __int_as_float(__float_as_int(__fmul_rn(fr, sc)) | (int)sgn);
+}
+
+// (s, c) += (ah + al)(bh + bl): TwoProduct of the high parts, the cross
+// terms into its error, TwoSum into s, both errors into c
+__device__ __forceinline__ void ds_dot2(float &s, float &c, float ah, float al, float bh, float bl) {
+    const float p = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+    c = __fadd_rn(c, __fadd_rn(err, e));
+    s = t;
+}
+
+constexpr int kDsV = 8;  // right-hand-side points per pass of a thread
+
+// One CTA per stored quadrant point, one thread per output row (component,
+// layer) for all its points and right-hand sides; the point's vectors are
+// staged as float pairs {re h, re l, im h, im l} in shared memory, the Green
+// block is read from global memory and split in registers. Sign flips of the
+// D_p symmetries negate the running sums around a block (exact).
+__global__ void __launch_bounds__(160) k_contract_ds(double2 *buf, const double2 *__restrict__ G, const OpDims d) {
+    extern __shared__ __align__(16) float4 sXd[];
+    const int nz = d.nz;
+    const int S = nz * (nz + 1) / 2, lda = nz + 1, A = nz * lda, Bs = 4 * S + 2 * A;
+    const int q = blockIdx.x;
+    const int a = q / (d.ny + 1), bq = q - a * (d.ny + 1);
+    const int n1 = 2 * d.ny;
+    const int kx[2] = {a, 2 * d.nx - a};
+    const int ky[2] = {bq, 2 * d.ny - bq};
+    const int nky = (bq == 0 || bq == d.ny) ? 1 : 2;
+    const int npts = ((a == 0 || a == d.nx) ? 1 : 2) * nky;
+    const int per = 3 * nz;
+    const int nv = npts * d.nrhs;
+    for (int t = threadIdx.x; t < nv * per; t += blockDim.x) {
+        const int v = t / per, e = t - v * per;
+        const int p = v / d.nrhs, rhs = v - p * d.nrhs;
+        const long pt = (long)kx[p / nky] * n1 + ky[p % nky];
+        const double2 x = buf[pt * d.B + rhs * per + e];
+        float4 o;
+        ds_split(x.x, o.x, o.y);
+        ds_split(x.y, o.z, o.w);
+        sXd[t] = o;
+    }
+    __syncthreads();
+    const int row = threadIdx.x;
+    if (row >= per) return;
+    const int cout = row / nz, i = row - cout * nz;
+    const double2 *gq = G + (long)q * Bs;
+    // per block: base of its Green component and the index kind
+    // (0 symmetric packed (i, j), 1 row i of a full nz x lda block, 2 column i)
+    const double2 *base[3];
+    int kind[3];
+    if (cout == 0) {
+        base[0] = gq, kind[0] = 0;               // Sxx
+        base[1] = gq + S, kind[1] = 0;           // Sxy
+        base[2] = gq + 4 * S, kind[2] = 1;       // Axz
+    } else if (cout == 1) {
+        base[0] = gq + S, kind[0] = 0;           // Sxy
+        base[1] = gq + 2 * S, kind[1] = 0;       // Syy
+        base[2] = gq + 4 * S + A, kind[2] = 1;   // Ayz
+    } else {
+        base[0] = gq + 4 * S, kind[0] = 2;       // Axz^T
+        base[1] = gq + 4 * S + A, kind[1] = 2;   // Ayz^T
+        base[2] = gq + 3 * S, kind[2] = 0;       // Szz
+    }
+    for (int v0 = 0; v0 < nv; v0 += kDsV) {
+        const int cnt = min(kDsV, nv - v0);
+        float sr[kDsV], cr[kDsV], si[kDsV], ci[kDsV];
+#pragma unroll
+        for (int u = 0; u < kDsV; u++) sr[u] = cr[u] = si[u] = ci[u] = 0.f;
+        for (int blk = 0; blk < 3; blk++) {
+            // the block's sign per point: cout 0: Sxy odd/odd, Axz odd in x;
+            // cout 1: Sxy odd/odd, Ayz odd in y; cout 2: -Axz^T, -Ayz^T even
+            float sg[kDsV];
+#pragma unroll
+            for (int u = 0; u < kDsV; u++) {
+                const int p = (v0 + u) / d.nrhs;
+                const bool mx = (p / nky) == 1, my = (p % nky) == 1;
+                bool flip = false;
+                if (cout == 0) flip = blk == 1 ? mx != my : (blk == 2 ? mx : false);
+                else if (cout == 1) flip = blk == 0 ? mx != my : (blk == 2 ? my : false);
+                else flip = blk == 0 ? !mx : (blk == 1 ? !my : false);
+                sg[u] = flip ? -1.f : 1.f;
+                sr[u] *= sg[u], cr[u] *= sg[u], si[u] *= sg[u], ci[u] *= sg[u];
+            }
+            const double2 *gb = base[blk];
+            const int kd = kind[blk];
+            const float4 *X = sXd + (long)v0 * per + blk * nz;
+            for (int j = 0; j < nz; j++) {
+                const int idx = kd == 0 ? sym_index(i, j) : (kd == 1 ? i * lda + j : j * lda + i);
+                const double2 g = __ldg(gb + idx);
+                float grh, grl, gih, gil;
+                ds_split(g.x, grh, grl);
+                ds_split(g.y, gih, gil);
+#pragma unroll
+                for (int u = 0; u < kDsV; u++) {
+                    if (u < cnt) {
+                        const float4 x = X[(long)u * per + j];
+                        ds_dot2(sr[u], cr[u], grh, grl, x.x, x.y);
+                        ds_dot2(sr[u], cr[u], -gih, -gil, x.z, x.w);
+                        ds_dot2(si[u], ci[u], grh, grl, x.z, x.w);
+                        ds_dot2(si[u], ci[u], gih, gil, x.x, x.y);
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kDsV; u++) sr[u] *= sg[u], cr[u] *= sg[u], si[u] *= sg[u], ci[u] *= sg[u];
+        }
+#pragma unroll
+        for (int u = 0; u < kDsV; u++) {
+            if (u < cnt) {
+                const int v = v0 + u;
+                const int p = v / d.nrhs, rhs = v - p * d.nrhs;
+                const long pt = (long)kx[p / nky] * n1 + ky[p % nky];
+                buf[pt * d.B + rhs * per + row] =
+                    make_double2((double)sr[u] + (double)cr[u], (double)si[u] + (double)ci[u]);
+            }
+        }
+    }
+}
+
+bool contract_ds_fits(int nz, int nrhs) {
+    return 3 * nz <= 160 && (size_t)4 * nrhs * 3 * nz * sizeof(float4) <= 96 * 1024;
+}
+
 static int threads_for(int items) { return items >= 256 ? 256 : (items >= 128 ? 128 : 64); }
 
 template <typename T>
@@ -398,6 +554,12 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
             launch_contract_mma(reinterpret_cast<float2 *>(buf), reinterpret_cast<const float2 *>(G), d, err, s);
         } else if (std::is_same<T, float>::value && err && contract_c64_fits(d.nz, d.nrhs)) {
             launch_contract_c64(reinterpret_cast<float2 *>(buf), reinterpret_cast<const float2 *>(G), d, err, s);
+        } else if (std::is_same<T, double>::value && d.ds && contract_ds_fits(d.nz, d.nrhs)) {
+            const int per = 3 * d.nz;
+            const size_t sm = (size_t)4 * d.nrhs * per * sizeof(float4);
+            set_smem<T>((const void *)k_contract_ds, sm);
+            k_contract_ds<<<(unsigned)gd.Q(), (per + 31) / 32 * 32, sm, s>>>(reinterpret_cast<double2 *>(buf),
+                                                                             reinterpret_cast<const double2 *>(G), d);
         } else if (sx + sg <= 200 * 1024) {
             set_smem<T>((const void *)k_contract<T, true>, sx + sg);
             k_contract<T, true><<<(unsigned)gd.Q(), thr, sx + sg, s>>>(buf, G, d);

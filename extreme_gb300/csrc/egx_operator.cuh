@@ -28,6 +28,7 @@ struct OpDims {
     int nx, ny, nz, nrhs;
     int B;       // batch of the spectral buffer: nrhs * 3 * nz
     long nvec;   // elements of one anomaly vector: nx*ny*3*nz
+    int ds = 0;  // complex128 apply: contraction in double-FP32 arithmetic
 };
 
 template <typename T>
@@ -43,6 +44,10 @@ template <typename T>
 void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, const C<T> *x, C<T> *y, C<T> *buf,
                     const C<T> *tw0, const C<T> *tw1, const FftPlan &p0, const FftPlan &p1, cudaStream_t s,
                     long *launches, Timers *timers = nullptr, int *err = nullptr);
+
+// the double-FP32 complex128 contraction covers 3 nz <= 160 and its staged
+// vectors fit in 96 KiB
+bool contract_ds_fits(int nz, int nrhs);
 
 // complex64 contraction with TMA-staged blocks (egx_contract.cu); `err`
 // receives EGX_ERR_TIMEOUT if a bounded wait expires.

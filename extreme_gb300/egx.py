@@ -23,7 +23,7 @@ PRECOND_GMRES, PRECOND_CALLBACK, PRECOND_NONE, PRECOND_LEARNED = 0, 1, 2, 3
 EXPORTS = [
     "egx_create", "egx_destroy", "egx_last_error", "egx_version", "egx_set_stream", "egx_launch_count",
     "egx_green_build", "egx_green_upload", "egx_green_download", "egx_green_free",
-    "egx_op_prepare", "egx_op_apply", "egx_op_apply_c64", "egx_fft2d",
+    "egx_op_prepare", "egx_op_apply", "egx_op_apply_ds", "egx_op_apply_c64", "egx_fft2d",
     "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products", "egx_dot_products_static",
     "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_read",
     "egx_level_fields", "egx_level_cache", "egx_mt_responses", "egx_wait_selftest",
@@ -104,6 +104,7 @@ def load(path=None):
     lib.egx_op_prepare.argtypes = [vp, vp, vp, vp, vp, i]
     lib.egx_op_apply.argtypes = [vp, vp, vp, i, i]
     lib.egx_op_apply_c64.argtypes = [vp, vp, vp, i, i]
+    lib.egx_op_apply_ds.argtypes = [vp, vp, vp, i, i]
     lib.egx_fft2d.argtypes = [vp, vp, i, i, i, i, i]
     lib.egx_fgmres_solve.argtypes = [vp, vp, vp, C.POINTER(GmresParams), C.POINTER(Result), i]
     lib.egx_mixed_solve.argtypes = [vp, vp, vp, C.POINTER(MixedParams), C.POINTER(Result), i]
@@ -215,6 +216,13 @@ class Context:
 
     def op_apply_dev(self, x_ptr, y_ptr, nrhs=1):
         self._check(self.lib.egx_op_apply(self.h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), nrhs, DEVICE))
+
+    def op_apply_ds(self, x, nrhs=1):
+        """Host arrays (complex128); the contraction in double-FP32."""
+        x = _c128(x)
+        y = np.empty_like(x)
+        self._check(self.lib.egx_op_apply_ds(self.h, _ptr(x), _ptr(y), nrhs, HOST))
+        return y
 
     def op_apply_c64(self, x, nrhs=1):
         x = np.ascontiguousarray(x, np.complex64)

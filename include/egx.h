@@ -152,6 +152,12 @@ int egx_op_prepare(egx_ctx *ctx, egx_green *g, const double *zeta, const double 
 int egx_op_apply(egx_ctx *ctx, const double *x, double *y, int nrhs, int where);
 /* Same in complex64 (interleaved floats) with the complex64 tensor. */
 int egx_op_apply_c64(egx_ctx *ctx, const float *x, float *y, int nrhs, int where);
+/* The complex128 apply with its block contraction in double-FP32
+ * arithmetic (Dot2 on float pairs, ~47 significant bits, no complex128 FMA):
+ * the apply the mixed form uses for its refinement residuals. Same
+ * arguments as egx_op_apply; nz <= 53 and 4 nrhs 3 nz float4 of staged
+ * vectors <= 96 KiB, else the complex128 contraction runs. */
+int egx_op_apply_ds(egx_ctx *ctx, const double *x, double *y, int nrhs, int where);
 
 /* ---- FFT (FftWrap plan_many_dft rank 2) -------------------------------- */
 /* In-place unnormalised 2-D DFT over (n0, n1) of `howmany` interleaved

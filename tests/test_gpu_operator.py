@@ -113,6 +113,28 @@ def test_c64_subblock_apply_matches_oracle(egx_ctx, nz):
     g.free()
 
 
+@pytest.mark.parametrize("nz,nrhs", [(48, 2), (48, 1), (7, 3), (2, 10)])
+def test_double_fp32_apply_matches_complex128(egx_ctx, nz, nrhs):
+    """The mixed form's residual apply (contraction as Dot2 on float pairs)
+    against the complex128 apply: <= 1e-12 relative per vector, ragged
+    edges (nx != ny), one to ten right-hand sides (passes of eight points)."""
+    from extreme_gb300.model import freq_to_omega, scaled_model
+    m = scaled_model(10, 6, nz, seed=5)
+    f = m.frequencies[1]
+    om = OmegaModel.build(m, f)
+    g = egx_ctx.green_build(m, freq_to_omega(f), 10, egx.PREC_MIXED)
+    egx_ctx.op_prepare(g, om.zeta, om.zeta0, m.layer_thickness, op.OP_A)
+    rng = np.random.default_rng(nz + nrhs)
+    n = m.nx * m.ny * 3 * m.nz
+    # magnitudes spread over many decades, as in a converged residual
+    xs = (rng.standard_normal((nrhs, n)) + 1j * rng.standard_normal((nrhs, n))) * 10.0 ** rng.uniform(-8, 2, (nrhs, n))
+    want = egx_ctx.op_apply(xs.reshape(-1), nrhs=nrhs)
+    got = egx_ctx.op_apply_ds(xs.reshape(-1), nrhs=nrhs)
+    for i in range(nrhs):
+        assert rel(got[i * n:(i + 1) * n], want[i * n:(i + 1) * n]) < 1e-12, i
+    g.free()
+
+
 def test_apply_before_prepare_is_state_error():
     ctx = egx.Context(0)
     with pytest.raises(egx.EgxError) as e:
