@@ -236,14 +236,15 @@ def run_ours(args, rank, world, local):
                                         mixed=mixed, where=egx.DEVICE,
                                         dev_ptrs=dict(zeta=zeta_d[k].data_ptr(), zeta0=zeta0_d[k].data_ptr(),
                                                       e0=e0_d[k].data_ptr(), jq=jq_d.data_ptr()))
-                ctx.level_fields_dev(m, omega, jq_d.data_ptr(), 2, e_d.data_ptr(), h_d.data_ptr(), z=0.0)
+                ctx.level_fields_dev(m, omega, jq_d.data_ptr(), 2, e_d.data_ptr(), h_d.data_ptr(), z=0.0,
+                                     precision=egx.PREC_MIXED)
                 e = e_d.cpu().numpy().view(np.complex128)
                 h = h_d.cpu().numpy().view(np.complex128)
             else:
                 z, z0 = host_in[k]
                 jq, _, res = ctx.solve_sources(g, z, z0, m.layer_thickness, host_e0[k], [0, 1],
                                                precision=egx.PREC_MIXED, mixed=mixed)
-                e, h = ctx.level_fields(m, omega, jq, z=0.0)
+                e, h = ctx.level_fields(m, omega, jq, z=0.0, precision=egx.PREC_MIXED)
             responses(k, e, h)
             return res
         finally:

@@ -75,6 +75,7 @@ struct egx_ctx {
     int lvl_capacity = kLevelSlots;
     unsigned long long lvl_clock = 0;
     long lvl_hits = 0, lvl_builds = 0;
+    int lvl_prec = EGX_PREC_FP64;  // EGX_PREC_MIXED: complex64 lateral FFT of the level tensors
 };
 
 // Body of a C entry point: returns EGX_OK, or the status of the exception

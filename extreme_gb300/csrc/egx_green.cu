@@ -782,9 +782,10 @@ __global__ void k_zero_rho(double2 *__restrict__ I, int nu, int ntrans, int nrad
 
 // Level tensor value of every cell of the full 2nx x 2ny offset grid for
 // transmitter layers [0, nt): buf[cell][nt] (cells without terms stay 0).
+template <typename O>
 __global__ void k_cells_level(const int *__restrict__ rowptr, const Term *__restrict__ terms,
                               const double2 *__restrict__ IA, const double2 *__restrict__ IB, int ntrans, int nseg,
-                              int ncell, double2 *__restrict__ buf) {
+                              int ncell, O *__restrict__ buf) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)ncell * ntrans) return;
     const int cell = (int)(idx / ntrans), t = (int)(idx - (long)cell * ntrans);
@@ -796,7 +797,12 @@ __global__ void k_cells_level(const int *__restrict__ rowptr, const Term *__rest
         acc.x = fma(tm.wa, a.x, fma(tm.wb, b.x, acc.x));
         acc.y = fma(tm.wa, a.y, fma(tm.wb, b.y, acc.y));
     }
-    buf[idx] = acc;
+    buf[idx] = cell_out<O>(acc);
+}
+
+__global__ void k_widen(const float2 *__restrict__ x, long n, double2 *__restrict__ y) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        y[i] = make_double2(x[i].x, x[i].y);
 }
 
 // Component tables of the level tensors, in the order of level_components:
@@ -1280,7 +1286,7 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
 int level_components(int kind) { return kind == 0 ? 8 : 7; }
 
 void build_level_green(const GreenModel &m, int n_hankels, double z, double shx, double shy, int kind, cudaStream_t s,
-                       DevBuf &out, long *launches, GreenWorkspace &w) {
+                       DevBuf &out, long *launches, GreenWorkspace &w, bool fft32) {
     EGX_CHECK(m.nx > 0 && m.ny > 0 && m.nz > 0 && m.dx > 0 && m.dy > 0, EGX_ERR_INVALID, "bad model dimensions");
     EGX_CHECK(kind == 0 || kind == 1, EGX_ERR_INVALID, "level tensor kind must be 0 (E) or 1 (H)");
     const int L = (int)m.bg_thick.size();
@@ -1436,15 +1442,37 @@ void build_level_green(const GreenModel &m, int n_hankels, double z, double shx,
     FftPlan p0 = make_fft_plan(n0), p1 = make_fft_plan(n1);
     {
         std::vector<double> t0 = twiddles(n0), t1 = twiddles(n1);
-        dev_upload(w.tw0, t0, s);
-        dev_upload(w.tw1, t1, s);
+        if (fft32) {
+            dev_upload(w.tw0_32, std::vector<float>(t0.begin(), t0.end()), s);
+            dev_upload(w.tw1_32, std::vector<float>(t1.begin(), t1.end()), s);
+            w.d_buf32.ensure(comp_elems * sizeof(float2));
+        } else {
+            dev_upload(w.tw0, t0, s);
+            dev_upload(w.tw1, t1, s);
+        }
     }
     for (int c = 0; c < ncomp; c++) {
         double2 *g = out.as<double2>() + (size_t)c * comp_elems;
         const long n = ncell * m.nz;
-        k_cells_level<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w.lrow[kind][c].as<int>(),
-                                                                  w.lterm[kind][c].as<Term>(), w.d_IA.as<double2>(),
-                                                                  w.d_IB.as<double2>(), ntrans, nseg, (int)ncell, g);
+        const int *rp = w.lrow[kind][c].as<int>();
+        const Term *tt = w.lterm[kind][c].as<Term>();
+        if (fft32) {
+            // face integrals in FP64 rounded to complex64 as written; the
+            // 2-D FFT in complex64; widened into the complex128 tensor
+            float2 *g32 = w.d_buf32.as<float2>();
+            k_cells_level<float2><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+                rp, tt, w.d_IA.as<double2>(), w.d_IB.as<double2>(), ntrans, nseg, (int)ncell, g32);
+            EGX_CUDA(cudaGetLastError());
+            fft_lines<float>(g32, n0, (long)n1 * m.nz, m.nz, m.nz, n1, n1, p1, w.tw1_32.as<float2>(), -1, s, launches);
+            fft_lines<float>(g32, n1, m.nz, (long)n1 * m.nz, m.nz, n0, n0, p0, w.tw0_32.as<float2>(), -1, s, launches);
+            k_widen<<<(unsigned)std::min<long>((n + 255) / 256, 152L * 16), 256, 0, s>>>(g32, n, g);
+            EGX_CUDA(cudaGetLastError());
+            if (launches) *launches += 2;
+            continue;
+        }
+        k_cells_level<double2><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(rp, tt, w.d_IA.as<double2>(),
+                                                                           w.d_IB.as<double2>(), ntrans, nseg,
+                                                                           (int)ncell, g);
         EGX_CUDA(cudaGetLastError());
         // PerformGreenTensorFft: the full 2-D transform of every layer column
         fft_lines<double>(g, n0, (long)n1 * m.nz, m.nz, m.nz, n1, n1, p1, w.tw1.as<double2>(), -1, s, launches);

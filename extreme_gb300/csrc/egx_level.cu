@@ -101,6 +101,14 @@ __global__ void k_level_extract(const double2 *__restrict__ out3, int nx, int ny
 
 extern "C" {
 
+int egx_set_level_precision(egx_ctx *ctx, int precision) {
+    if (!ctx) return EGX_ERR_INVALID;
+    if (precision != EGX_PREC_FP64 && precision != EGX_PREC_MIXED)
+        return fail(ctx, EGX_ERR_INVALID, "unknown level precision");
+    ctx->lvl_prec = precision;
+    return EGX_OK;
+}
+
 int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_hankels, double z, double shift_x,
                      double shift_y, const double *jq, int nsrc, double *e, double *h, int where) {
     if (!ctx) return EGX_ERR_INVALID;
@@ -116,7 +124,8 @@ int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_h
         ensure_twiddles(ctx, n0, n1);
         // level tensors: reuse a cached pair or build into the least recently used slot
         std::vector<double> key = {(double)nx, (double)ny, (double)nz, model->dx, model->dy, omega,
-                                   (double)n_hankels, z, shift_x, shift_y, (double)model->n_bg, model->zero_air_level};
+                                   (double)n_hankels, z, shift_x, shift_y, (double)model->n_bg, model->zero_air_level,
+                                   (double)ctx->lvl_prec};
         key.insert(key.end(), model->layer_depth, model->layer_depth + nz);
         key.insert(key.end(), model->layer_thickness, model->layer_thickness + nz);
         key.insert(key.end(), model->bg_thickness, model->bg_thickness + model->n_bg);
@@ -134,8 +143,9 @@ int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_h
                 if (ctx->lvl_cache[i].used < ctx->lvl_cache[slot].used) slot = i;
             egx_ctx::LevelEntry &L = ctx->lvl_cache[slot];
             L.key.clear();  // not valid until both tensors are built
-            build_level_green(gm, n_hankels, z, shift_x, shift_y, 0, s, L.g[0], &ctx->launches, ctx->gws);
-            build_level_green(gm, n_hankels, z, shift_x, shift_y, 1, s, L.g[1], &ctx->launches, ctx->gws);
+            const bool fft32 = ctx->lvl_prec == EGX_PREC_MIXED;
+            build_level_green(gm, n_hankels, z, shift_x, shift_y, 0, s, L.g[0], &ctx->launches, ctx->gws, fft32);
+            build_level_green(gm, n_hankels, z, shift_x, shift_y, 1, s, L.g[1], &ctx->launches, ctx->gws, fft32);
             if (ctx->lvl_capacity > 0) L.key = key;
             ctx->lvl_builds++;
         }

@@ -26,7 +26,7 @@ EXPORTS = [
     "egx_op_prepare", "egx_op_apply", "egx_op_apply_ds", "egx_op_apply_c64", "egx_fft2d",
     "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products", "egx_dot_products_static",
     "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_read",
-    "egx_level_fields", "egx_level_cache", "egx_mt_responses", "egx_wait_selftest",
+    "egx_level_fields", "egx_level_cache", "egx_set_level_precision", "egx_mt_responses", "egx_wait_selftest",
     "egx_net_create", "egx_net_free", "egx_net_size", "egx_net_params", "egx_net_set_model", "egx_net_loss_grad",
     "egx_net_adam", "egx_net_apply", "egx_learned_stats",
 ]
@@ -118,6 +118,7 @@ def load(path=None):
     lib.egx_level_fields.argtypes = [vp, C.POINTER(Model), d, i, d, d, d, vp, i, vp, vp, i]
     lib.egx_mt_responses.argtypes = [vp, vp, vp, vp, C.c_long, d, vp, vp, vp]
     lib.egx_level_cache.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_long)]
+    lib.egx_set_level_precision.argtypes = [vp, i]
     lib.egx_wait_selftest.argtypes = [vp, d]
     lib.egx_net_create.argtypes = [vp, i, i, i, i, i, C.c_uint, C.POINTER(vp)]
     lib.egx_net_free.argtypes = [vp, vp]
@@ -347,9 +348,16 @@ class Context:
         self._check(self.lib.egx_level_cache(self.h, int(capacity), C.byref(hits), C.byref(builds)))
         return hits.value, builds.value
 
-    def level_fields(self, model, omega, jq, z=0.0, shift_x=0.0, shift_y=0.0, n_hankels=10):
+    def set_level_precision(self, precision):
+        """PREC_FP64 (default) or PREC_MIXED (complex64 lateral FFT of the
+        level tensors) for the level tensors built from now on."""
+        self._check(self.lib.egx_set_level_precision(self.h, int(precision)))
+
+    def level_fields(self, model, omega, jq, z=0.0, shift_x=0.0, shift_y=0.0, n_hankels=10, precision=PREC_FP64):
         """Anomalous E and H at the observation level z for jq [nsrc, N]
-        (host arrays): returns (e, h), each [nsrc, nx, ny, 3] complex128."""
+        (host arrays): returns (e, h), each [nsrc, nx, ny, 3] complex128.
+        precision: of the level tensors (egx_set_level_precision)."""
+        self.set_level_precision(precision)
         jq = _c128(jq).reshape(-1, model.nx * model.ny * 3 * model.nz)
         nsrc = jq.shape[0]
         e = np.empty((nsrc, model.nx, model.ny, 3), np.complex128)
@@ -360,8 +368,9 @@ class Context:
         return e, h
 
     def level_fields_dev(self, model, omega, jq_ptr, nsrc, e_ptr, h_ptr, z=0.0, shift_x=0.0, shift_y=0.0,
-                         n_hankels=10):
+                         n_hankels=10, precision=PREC_FP64):
         """egx_level_fields on device pointers (jq [nsrc][N], e/h [nsrc][nx][ny][3])."""
+        self.set_level_precision(precision)
         ms = model_struct(model)
         self._check(self.lib.egx_level_fields(self.h, C.byref(ms.s), omega, n_hankels, z, shift_x, shift_y,
                                               C.c_void_p(jq_ptr), nsrc, C.c_void_p(e_ptr), C.c_void_p(h_ptr),

@@ -138,10 +138,11 @@ class Mt3DForwardSolver:
         """Total fields of both polarisations at the level and the MT
         responses (``Mt3DForwardSolver`` observation path:
         ``AtoOCalculator`` anomalous fields + plane-wave normal fields,
-        ``Mt3DForwardSolver.cs:300-337``)."""
+        ``Mt3DForwardSolver.cs:300-337``). The level tensors are built in the
+        solver's precision (the mixed form: complex64 lateral FFT)."""
         omega = freq_to_omega(frequency)
         ea, ha = self.ctx.level_fields(model, omega, jq, z=z, shift_x=shift_x, shift_y=shift_y,
-                                       n_hankels=self.settings.number_of_hankels)
+                                       n_hankels=self.settings.number_of_hankels, precision=self.precision)
         e_n, h_n = egx.plane_wave(model, omega, z)
         e = ea.copy()
         h = ha.copy()

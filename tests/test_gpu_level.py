@@ -46,6 +46,29 @@ def test_level_fields_match_oracle(egx_ctx, z, sx, sy):
         assert rel(h[i], atoo.anomaly_field(om, gh, jq[i], "H")) < 1e-10, (i, "H")
 
 
+@pytest.mark.parametrize("shape", [(8, 6, 3), (32, 32, 8)])
+def test_mixed_level_tensors_match_fp64(egx_ctx, shape):
+    """Level tensors with the complex64 lateral FFT (the mixed form): fields
+    within 1e-6 of the FP64 build; the precision is part of the level
+    cache's key."""
+    from extreme_gb300.model import freq_to_omega, scaled_model
+    m = scaled_model(*shape, seed=4)
+    omega = freq_to_omega(m.frequencies[1])
+    rng = np.random.default_rng(3)
+    n = m.nx * m.ny * 3 * m.nz
+    jq = rng.standard_normal((2, n)) + 1j * rng.standard_normal((2, n))
+    egx_ctx.level_cache(4)
+    h0, b0 = egx_ctx.level_cache()
+    e64, h64 = egx_ctx.level_fields(m, omega, jq, z=0.0)
+    e32, h32 = egx_ctx.level_fields(m, omega, jq, z=0.0, precision=egx.PREC_MIXED)
+    e32b, _ = egx_ctx.level_fields(m, omega, jq, z=0.0, precision=egx.PREC_MIXED)
+    h1, b1 = egx_ctx.level_cache()
+    assert (h1 - h0, b1 - b0) == (1, 2)
+    np.testing.assert_array_equal(e32, e32b)
+    assert rel(e32, e64) < 1e-6 and rel(h32, h64) < 1e-6, (rel(e32, e64), rel(h32, h64))
+    assert rel(e32, e64) > 0   # the complex64 FFT ran
+
+
 def test_surface_responses_match_oracle(egx_ctx):
     m = small_model()
     f = 0.1
