@@ -27,6 +27,7 @@
 #include <mutex>
 #include <set>
 
+#include "egx_ds.cuh"
 #include "egx_green.cuh"
 #include "egx_operator.cuh"
 #include "hankel_ndec40.inc"
@@ -316,9 +317,11 @@ __global__ void k_hankel(const double2 *__restrict__ U, int nu, int ntrans, long
     I[((long)u * ntrans + tr) * nrad + gidx[i]] = dmk(sx / den, sy / den);
 }
 
-// IA/IB[u][seg][trans]
+// IA/IB[u][seg][trans]; with IA32/IB32 also as float pairs {re h, re l,
+// im h, im l} for the double-FP32 face sums
 __global__ void k_segments(const double2 *__restrict__ I, int nu, int ntrans, int nrad, const double *__restrict__ radii,
-                           double2 *__restrict__ IA, double2 *__restrict__ IB) {
+                           double2 *__restrict__ IA, double2 *__restrict__ IB, float4 *__restrict__ IA32,
+                           float4 *__restrict__ IB32) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int nseg = nrad - 1;
     if (idx >= (long)nu * nseg * ntrans) return;
@@ -334,6 +337,15 @@ __global__ void k_segments(const double2 *__restrict__ I, int nu, int ntrans, in
     long o = ((long)u * nseg + sg) * ntrans + tr;
     IA[o] = a;
     IB[o] = bb;
+    if (IA32) {
+        float4 fa, fb;
+        ds_split(a.x, fa.x, fa.y);
+        ds_split(a.y, fa.z, fa.w);
+        ds_split(bb.x, fb.x, fb.y);
+        ds_split(bb.y, fb.z, fb.w);
+        IA32[o] = fa;
+        IB32[o] = fb;
+    }
 }
 
 struct Term {
@@ -385,6 +397,64 @@ __global__ void k_cells(const int *__restrict__ rowptr, const Term *__restrict__
         buf[((long)(n0 - i) * n1) * tc + t] = cell_out<O>(dscal((double)xs, acc));
     } else if (j >= 1) {
         buf[((long)(n1 - j)) * tc + t] = cell_out<O>(dscal((double)ys, acc));
+    }
+}
+
+// k_cells for the mixed form: the same face sums as Dot2 on float pairs
+// (double-FP32, the FP32 pipes), rounded to complex64. The block's cell
+// terms are split into shared memory once per chunk.
+constexpr int kCellChunk = 128;
+__global__ void __launch_bounds__(128) k_cells_ds(const int *__restrict__ rowptr, const Term *__restrict__ terms,
+                                                  const float4 *__restrict__ IA, const float4 *__restrict__ IB,
+                                                  int ntrans, int nseg, int nx, int ny, int t0, int tc, int xs,
+                                                  int ys, int compact, float2 *__restrict__ buf) {
+    __shared__ float4 sw[kCellChunk];
+    __shared__ long so[kCellChunk];
+    const int cell = blockIdx.x;
+    const int i = cell / ny, j = cell - (cell / ny) * ny;
+    const int t = blockIdx.y * blockDim.x + threadIdx.x;
+    float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+    const int e0 = rowptr[cell], e1 = rowptr[cell + 1];
+    for (int c0 = e0; c0 < e1; c0 += kCellChunk) {
+        const int cnt = min(kCellChunk, e1 - c0);
+        __syncthreads();
+        if ((int)threadIdx.x < cnt) {
+            const Term tm = terms[c0 + threadIdx.x];
+            float4 w;
+            ds_split(tm.wa, w.x, w.y);
+            ds_split(tm.wb, w.z, w.w);
+            sw[threadIdx.x] = w;
+            so[threadIdx.x] = ((long)tm.src * nseg + tm.seg) * ntrans + t0;
+        }
+        __syncthreads();
+        if (t < tc) {
+            for (int e = 0; e < cnt; e++) {
+                const float4 w = sw[e];
+                const float4 a = IA[so[e] + t], b = IB[so[e] + t];
+                ds_dot2(sr, cr, w.x, w.y, a.x, a.y);
+                ds_dot2(sr, cr, w.z, w.w, b.x, b.y);
+                ds_dot2(si, ci, w.x, w.y, a.z, a.w);
+                ds_dot2(si, ci, w.z, w.w, b.z, b.w);
+            }
+        }
+    }
+    if (t >= tc) return;
+    const float2 v = make_float2(__fadd_rn(sr, cr), __fadd_rn(si, ci));
+    if (compact) {
+        buf[((long)i * (ny + 1) + j) * tc + t] = v;
+        return;
+    }
+    const int n0 = 2 * nx, n1 = 2 * ny;
+    const float fx = (float)xs, fy = (float)ys;
+    buf[((long)i * n1 + j) * tc + t] = v;
+    if (i >= 1 && j >= 1) {
+        buf[((long)(n0 - i) * n1 + j) * tc + t] = make_float2(fx * v.x, fx * v.y);
+        buf[((long)i * n1 + (n1 - j)) * tc + t] = make_float2(fy * v.x, fy * v.y);
+        buf[((long)(n0 - i) * n1 + (n1 - j)) * tc + t] = make_float2(fx * fy * v.x, fx * fy * v.y);
+    } else if (i >= 1) {
+        buf[((long)(n0 - i) * n1) * tc + t] = make_float2(fx * v.x, fx * v.y);
+    } else if (j >= 1) {
+        buf[((long)(n1 - j)) * tc + t] = make_float2(fy * v.x, fy * v.y);
     }
 }
 
@@ -800,6 +870,29 @@ __global__ void k_cells_level(const int *__restrict__ rowptr, const Term *__rest
     buf[idx] = cell_out<O>(acc);
 }
 
+// k_cells_level for the mixed form: Dot2 on float pairs, rounded to complex64
+__global__ void k_cells_level_ds(const int *__restrict__ rowptr, const Term *__restrict__ terms,
+                                 const float4 *__restrict__ IA, const float4 *__restrict__ IB, int ntrans, int nseg,
+                                 int ncell, float2 *__restrict__ buf) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)ncell * ntrans) return;
+    const int cell = (int)(idx / ntrans), t = (int)(idx - (long)cell * ntrans);
+    float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+    for (int e = rowptr[cell]; e < rowptr[cell + 1]; e++) {
+        const Term tm = terms[e];
+        const long o = ((long)tm.src * nseg + tm.seg) * ntrans + t;
+        float wah, wal, wbh, wbl;
+        ds_split(tm.wa, wah, wal);
+        ds_split(tm.wb, wbh, wbl);
+        const float4 a = IA[o], b = IB[o];
+        ds_dot2(sr, cr, wah, wal, a.x, a.y);
+        ds_dot2(sr, cr, wbh, wbl, b.x, b.y);
+        ds_dot2(si, ci, wah, wal, a.z, a.w);
+        ds_dot2(si, ci, wbh, wbl, b.z, b.w);
+    }
+    buf[idx] = make_float2(__fadd_rn(sr, cr), __fadd_rn(si, ci));
+}
+
 __global__ void k_widen(const float2 *__restrict__ x, long n, double2 *__restrict__ y) {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
         y[i] = make_double2(x[i].x, x[i].y);
@@ -1175,10 +1268,17 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
         const int nseg = nrad - 1;
         d_IA.ensure((size_t)nu * nseg * ntrans * sizeof(double2));
         d_IB.ensure((size_t)nu * nseg * ntrans * sizeof(double2));
+        // the mixed form's face sums run in double-FP32 on float pairs
+        const bool face_ds = lateral_fft32 && fft_lines_sym_ok(2 * m.nx) && fft_lines_sym_ok(2 * m.ny);
+        if (face_ds) {
+            w.d_IA32.ensure((size_t)nu * nseg * ntrans * sizeof(float4));
+            w.d_IB32.ensure((size_t)nu * nseg * ntrans * sizeof(float4));
+        }
         {
             long n = (long)nu * nseg * ntrans;
-            k_segments<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_I.as<double2>(), nu, ntrans, nrad, radii_dev,
-                                                                   d_IA.as<double2>(), d_IB.as<double2>());
+            k_segments<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+                d_I.as<double2>(), nu, ntrans, nrad, radii_dev, d_IA.as<double2>(), d_IB.as<double2>(),
+                face_ds ? w.d_IA32.as<float4>() : nullptr, face_ds ? w.d_IB32.as<float4>() : nullptr);
             if (launches) *launches += 1;
         }
         EGX_CUDA(cudaGetLastError());
@@ -1233,9 +1333,9 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
                 dim3 grid(m.nx * m.ny, (tcc + 127) / 128);
                 int ev = tm ? tm->begin(EGX_K_GREEN_CELLS, s) : -1;
                 if (fft32)
-                    k_cells<float2><<<grid, 128, 0, s>>>(drow, dterm, d_IA.as<double2>(), d_IB.as<double2>(), ntrans,
-                                                         nseg, m.nx, m.ny, t0, tcc, px[c], py[c], 1,
-                                                         w.d_buf32.as<float2>());
+                    k_cells_ds<<<grid, 128, 0, s>>>(drow, dterm, w.d_IA32.as<float4>(), w.d_IB32.as<float4>(),
+                                                    ntrans, nseg, m.nx, m.ny, t0, tcc, px[c], py[c], 1,
+                                                    w.d_buf32.as<float2>());
                 else
                     k_cells<double2><<<grid, 128, 0, s>>>(drow, dterm, d_IA.as<double2>(), d_IB.as<double2>(), ntrans,
                                                           nseg, m.nx, m.ny, t0, tcc, px[c], py[c], compact ? 1 : 0,
@@ -1411,10 +1511,15 @@ void build_level_green(const GreenModel &m, int n_hankels, double z, double shx,
     const int nseg = nrad - 1;
     w.d_IA.ensure((size_t)nu * nseg * ntrans * sizeof(double2));
     w.d_IB.ensure((size_t)nu * nseg * ntrans * sizeof(double2));
+    if (fft32) {
+        w.d_IA32.ensure((size_t)nu * nseg * ntrans * sizeof(float4));
+        w.d_IB32.ensure((size_t)nu * nseg * ntrans * sizeof(float4));
+    }
     {
         const long n = (long)nu * nseg * ntrans;
-        k_segments<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w.d_I.as<double2>(), nu, ntrans, nrad, radii_dev,
-                                                               w.d_IA.as<double2>(), w.d_IB.as<double2>());
+        k_segments<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+            w.d_I.as<double2>(), nu, ntrans, nrad, radii_dev, w.d_IA.as<double2>(), w.d_IB.as<double2>(),
+            fft32 ? w.d_IA32.as<float4>() : nullptr, fft32 ? w.d_IB32.as<float4>() : nullptr);
         if (launches) *launches += 1;
     }
     EGX_CUDA(cudaGetLastError());
@@ -1457,11 +1562,11 @@ void build_level_green(const GreenModel &m, int n_hankels, double z, double shx,
         const int *rp = w.lrow[kind][c].as<int>();
         const Term *tt = w.lterm[kind][c].as<Term>();
         if (fft32) {
-            // face integrals in FP64 rounded to complex64 as written; the
+            // face sums in double-FP32 rounded to complex64 as written; the
             // 2-D FFT in complex64; widened into the complex128 tensor
             float2 *g32 = w.d_buf32.as<float2>();
-            k_cells_level<float2><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
-                rp, tt, w.d_IA.as<double2>(), w.d_IB.as<double2>(), ntrans, nseg, (int)ncell, g32);
+            k_cells_level_ds<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+                rp, tt, w.d_IA32.as<float4>(), w.d_IB32.as<float4>(), ntrans, nseg, (int)ncell, g32);
             EGX_CUDA(cudaGetLastError());
             fft_lines<float>(g32, n0, (long)n1 * m.nz, m.nz, m.nz, n1, n1, p1, w.tw1_32.as<float2>(), -1, s, launches);
             fft_lines<float>(g32, n1, m.nz, (long)n1 * m.nz, m.nz, n0, n0, p0, w.tw0_32.as<float2>(), -1, s, launches);

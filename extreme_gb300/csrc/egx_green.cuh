@@ -33,6 +33,7 @@ struct GreenBuildStats {
 struct GreenWorkspace {
     DevBuf d_lam, d_lay, d_trans, d_U, d_I, d_rho, d_gidx, d_flags, d_neg, d_radii, d_IA, d_IB, d_buf, tw0, tw1;
     DevBuf d_buf32, tw0_32, tw1_32;  // the complex64 lateral FFT of the mixed form
+    DevBuf d_IA32, d_IB32;           // its face-sum coefficients as float pairs
     std::vector<double> key;  // nx, ny, dx, dy and the radii of the cached term lists
     DevBuf rowptr[6], terms[6];
     long nterms[6] = {};
