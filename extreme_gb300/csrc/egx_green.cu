@@ -893,10 +893,6 @@ __global__ void k_cells_level_ds(const int *__restrict__ rowptr, const Term *__r
     buf[idx] = make_float2(__fadd_rn(sr, cr), __fadd_rn(si, ci));
 }
 
-__global__ void k_widen(const float2 *__restrict__ x, long n, double2 *__restrict__ y) {
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        y[i] = make_double2(x[i].x, x[i].y);
-}
 
 // Component tables of the level tensors, in the order of level_components:
 // E: xx yy zz xy xz yz zx zy; H: xx yx xy xz yz zx zy. QSigns (QSign.cs:31-39)
@@ -1542,7 +1538,7 @@ void build_level_green(const GreenModel &m, int n_hankels, double z, double shx,
     }
     const long ncell = 4L * m.nx * m.ny;
     const size_t comp_elems = (size_t)ncell * m.nz;
-    out.ensure((size_t)ncomp * comp_elems * sizeof(double2));
+    out.ensure((size_t)ncomp * comp_elems * (fft32 ? sizeof(float2) : sizeof(double2)));
     const int n0 = 2 * m.nx, n1 = 2 * m.ny;
     FftPlan p0 = make_fft_plan(n0), p1 = make_fft_plan(n1);
     {
@@ -1550,31 +1546,28 @@ void build_level_green(const GreenModel &m, int n_hankels, double z, double shx,
         if (fft32) {
             dev_upload(w.tw0_32, std::vector<float>(t0.begin(), t0.end()), s);
             dev_upload(w.tw1_32, std::vector<float>(t1.begin(), t1.end()), s);
-            w.d_buf32.ensure(comp_elems * sizeof(float2));
         } else {
             dev_upload(w.tw0, t0, s);
             dev_upload(w.tw1, t1, s);
         }
     }
     for (int c = 0; c < ncomp; c++) {
-        double2 *g = out.as<double2>() + (size_t)c * comp_elems;
         const long n = ncell * m.nz;
         const int *rp = w.lrow[kind][c].as<int>();
         const Term *tt = w.lterm[kind][c].as<Term>();
         if (fft32) {
-            // face sums in double-FP32 rounded to complex64 as written; the
-            // 2-D FFT in complex64; widened into the complex128 tensor
-            float2 *g32 = w.d_buf32.as<float2>();
+            // face sums in double-FP32 rounded to complex64 as written, the
+            // 2-D FFT in complex64, the tensor kept in complex64
+            float2 *g32 = out.as<float2>() + (size_t)c * comp_elems;
             k_cells_level_ds<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
                 rp, tt, w.d_IA32.as<float4>(), w.d_IB32.as<float4>(), ntrans, nseg, (int)ncell, g32);
             EGX_CUDA(cudaGetLastError());
             fft_lines<float>(g32, n0, (long)n1 * m.nz, m.nz, m.nz, n1, n1, p1, w.tw1_32.as<float2>(), -1, s, launches);
             fft_lines<float>(g32, n1, m.nz, (long)n1 * m.nz, m.nz, n0, n0, p0, w.tw0_32.as<float2>(), -1, s, launches);
-            k_widen<<<(unsigned)std::min<long>((n + 255) / 256, 152L * 16), 256, 0, s>>>(g32, n, g);
-            EGX_CUDA(cudaGetLastError());
-            if (launches) *launches += 2;
+            if (launches) *launches += 1;
             continue;
         }
+        double2 *g = out.as<double2>() + (size_t)c * comp_elems;
         k_cells_level<double2><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(rp, tt, w.d_IA.as<double2>(),
                                                                            w.d_IB.as<double2>(), ntrans, nseg,
                                                                            (int)ncell, g);

@@ -51,9 +51,9 @@ int level_components(int kind);
 // Build the spectral anomaly-to-observation-level tensor of one kind at depth
 // z with the level's lateral shift, in FP64 on the device
 // (AtoOLevelGreenTensorCalculator.cs:21-126, AtoOCalculator.cs:120-176):
-// out = [component][2nx][2ny][nz] complex128. With fft32 the face
-// integrals (FP64) are rounded to complex64 and the 2-D FFT runs in
-// complex64 (the mixed form's level tensors).
+// out = [component][2nx][2ny][nz] complex128. With fft32 (the mixed form's
+// level tensors) the face sums run in double-FP32, are rounded to complex64,
+// and the 2-D FFT and `out` are complex64.
 void build_level_green(const GreenModel &m, int n_hankels, double z, double shift_x, double shift_y, int kind,
                        cudaStream_t s, DevBuf &out, long *launches, GreenWorkspace &ws, bool fft32 = false);
 

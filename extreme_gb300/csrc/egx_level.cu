@@ -1,7 +1,8 @@
 // Fields at an observation level and the MT responses.
 //
 // egx_level_fields builds the anomaly-to-observation-level tensors of E and H
-// in FP64 on the device (build_level_green, egx_green.cu;
+// on the device, in FP64 or, for the mixed form, with double-FP32 face sums
+// and complex64 FFTs and storage (build_level_green, egx_green.cu;
 // AtoOLevelGreenTensorCalculator.cs:21-126) and convolves them with jQ
 // (ToOCalculator.CalculateAnomalyField, ToOCalculator.cs:21-125):
 //   k_level_pad + 2-D DFT   jQ into the zero-padded [2nx][2ny][3nz] buffer
@@ -17,10 +18,96 @@
 #include <complex>
 
 #include "egx_ctx.cuh"
+#include "egx_ds.cuh"
 
 using namespace egx;
 
 namespace {
+
+// the mixed form's jQ, rounded to complex64 into the padded buffer
+__global__ void k_level_pad32(const double2 *__restrict__ jq, int nx, int ny, int per, float2 *__restrict__ buf) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)nx * ny * per) return;
+    const long cell = idx / per;
+    const int b = (int)(idx - cell * per);
+    const int i = (int)(cell / ny), j = (int)(cell - (long)i * ny);
+    const double2 v = jq[idx];
+    buf[((long)i * 2 * ny + j) * per + b] = make_float2((float)v.x, (float)v.y);
+}
+
+// (s, c) += a b for floats a, b: the product error-free (FMA), the sum
+// compensated (TwoSum)
+__device__ __forceinline__ void ds_mac(float &s, float &c, float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
+    s = t;
+}
+
+struct DsC {
+    float rs = 0.f, rc = 0.f, is = 0.f, ic = 0.f;
+    // += sign * g * x
+    __device__ __forceinline__ void mac(float2 g, float2 x, float sign) {
+        ds_mac(rs, rc, sign * g.x, x.x);
+        ds_mac(rs, rc, -sign * g.y, x.y);
+        ds_mac(is, ic, sign * g.x, x.y);
+        ds_mac(is, ic, sign * g.y, x.x);
+    }
+    __device__ __forceinline__ double2 value() const {
+        return make_double2((double)rs + (double)rc, (double)is + (double)ic);
+    }
+};
+
+// k_level_contract for the mixed form: complex64 spectra and level tensors,
+// products and sums exact to ~47 bits (Dot2), the result in complex128
+__global__ void k_level_contract_ds(const float2 *__restrict__ X, const float2 *__restrict__ G, long P, int nz,
+                                    int kind, double2 *__restrict__ out) {
+    const long p = (long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (p >= P) return;
+    const float2 *x = X + p * 3 * nz;
+    const size_t cs = (size_t)P * nz;
+    const float2 *g = G + p * nz;
+    DsC ax, ay, az;
+    for (int k = lane; k < nz; k += 32) {
+        const float2 sx = x[k], sy = x[nz + k], sz = x[2 * nz + k];
+        auto gc = [&](int c) { return g[c * cs + k]; };
+        if (kind == 0) {
+            ax.mac(gc(0), sx, 1.f);
+            ax.mac(gc(3), sy, 1.f);
+            ax.mac(gc(4), sz, 1.f);
+            ay.mac(gc(3), sx, 1.f);
+            ay.mac(gc(1), sy, 1.f);
+            ay.mac(gc(5), sz, 1.f);
+            az.mac(gc(6), sx, 1.f);
+            az.mac(gc(7), sy, 1.f);
+            az.mac(gc(2), sz, 1.f);
+        } else {
+            ax.mac(gc(0), sx, -1.f);
+            ax.mac(gc(2), sy, -1.f);
+            ax.mac(gc(3), sz, -1.f);
+            ay.mac(gc(1), sx, 1.f);
+            ay.mac(gc(0), sy, 1.f);
+            ay.mac(gc(4), sz, 1.f);
+            az.mac(gc(5), sx, -1.f);
+            az.mac(gc(6), sy, 1.f);
+        }
+    }
+    double2 v[3] = {ax.value(), ay.value(), az.value()};
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            v[c].x += __shfl_xor_sync(0xffffffffu, v[c].x, o);
+            v[c].y += __shfl_xor_sync(0xffffffffu, v[c].y, o);
+        }
+    if (lane == 0) {
+        out[p * 3] = v[0];
+        out[p * 3 + 1] = v[1];
+        out[p * 3 + 2] = v[2];
+    }
+}
 
 __global__ void k_level_pad(const double2 *__restrict__ jq, int nx, int ny, int per, double2 *__restrict__ buf) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -160,6 +247,8 @@ int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_h
         }
         double2 *X = ctx->lvl_x.as<double2>(), *O = ctx->lvl_out.as<double2>();
         const double2 *tw0 = ctx->tw0_64.as<double2>(), *tw1 = ctx->tw1_64.as<double2>();
+        const float2 *tw0_32 = ctx->tw0_32.as<float2>(), *tw1_32 = ctx->tw1_32.as<float2>();
+        const bool mixed = ctx->lvl_prec == EGX_PREC_MIXED;
         for (int i = 0; i < nsrc; i++) {
             const double2 *src;
             if (where == EGX_DEVICE) {
@@ -169,14 +258,28 @@ int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_h
                                          cudaMemcpyHostToDevice, s));
                 src = ctx->lvl_in.as<double2>();
             }
-            k_level_pad<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(src, nx, ny, per, X);
-            EGX_CUDA(cudaGetLastError());
-            // forward DFT: y over the nx data rows (ny loaded), then x over all columns (nx loaded)
-            fft_lines<double>(X, nx, (long)n1 * per, per, per, ny, n1, ctx->p1, tw1, -1, s, &ctx->launches);
-            fft_lines<double>(X, n1, per, (long)n1 * per, per, nx, n0, ctx->p0, tw0, -1, s, &ctx->launches);
+            if (mixed) {
+                // the mixed form: jQ's spectrum in complex64 against the
+                // complex64 level tensors
+                float2 *X32 = ctx->lvl_x.as<float2>();
+                k_level_pad32<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(src, nx, ny, per, X32);
+                EGX_CUDA(cudaGetLastError());
+                fft_lines<float>(X32, nx, (long)n1 * per, per, per, ny, n1, ctx->p1, tw1_32, -1, s, &ctx->launches);
+                fft_lines<float>(X32, n1, per, (long)n1 * per, per, nx, n0, ctx->p0, tw0_32, -1, s, &ctx->launches);
+            } else {
+                k_level_pad<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(src, nx, ny, per, X);
+                EGX_CUDA(cudaGetLastError());
+                // forward DFT: y over the nx data rows (ny loaded), then x over all columns (nx loaded)
+                fft_lines<double>(X, nx, (long)n1 * per, per, per, ny, n1, ctx->p1, tw1, -1, s, &ctx->launches);
+                fft_lines<double>(X, n1, per, (long)n1 * per, per, nx, n0, ctx->p0, tw0, -1, s, &ctx->launches);
+            }
             for (int kind = 0; kind < 2; kind++) {
-                k_level_contract<<<(unsigned)((P + 7) / 8), 256, 0, s>>>(X, lv.g[kind].as<double2>(), P, nz,
-                                                                         kind, O);
+                if (mixed)
+                    k_level_contract_ds<<<(unsigned)((P + 7) / 8), 256, 0, s>>>(
+                        ctx->lvl_x.as<float2>(), lv.g[kind].as<float2>(), P, nz, kind, O);
+                else
+                    k_level_contract<<<(unsigned)((P + 7) / 8), 256, 0, s>>>(X, lv.g[kind].as<double2>(), P, nz,
+                                                                             kind, O);
                 EGX_CUDA(cudaGetLastError());
                 // inverse DFT of the 3 columns: x keeping rows < nx, then y keeping j < ny
                 fft_lines<double>(O, n1, 3, (long)n1 * 3, 3, n0, nx, ctx->p0, tw0, +1, s, &ctx->launches);
