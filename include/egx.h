@@ -279,11 +279,12 @@ int egx_level_fields(egx_ctx *ctx, const egx_model *model, double omega, int n_h
  * setting it drops the cached levels. hits, builds (may be NULL): counts of
  * reused and built levels since the context was created. */
 int egx_level_cache(egx_ctx *ctx, int capacity, long *hits, long *builds);
-/* Precision of the level tensors that egx_level_fields builds from now on
- * (part of the level cache's key): EGX_PREC_FP64 (default, the reference's
- * arithmetic) or EGX_PREC_MIXED, whose FP64 face integrals are rounded to
- * complex64 for a complex64 2-D FFT and widened back (fields within ~1e-6
- * of the FP64 build; the mixed form's solve is only 1e-6-accurate). */
+/* Precision of egx_level_fields from now on (part of the level cache's
+ * key): EGX_PREC_FP64 (default, the reference's arithmetic) or
+ * EGX_PREC_MIXED: face sums in double-FP32 rounded to complex64, level
+ * tensors kept in complex64 (2-D FFT and storage, half the cache memory),
+ * jQ's spectrum in complex64, layer sums as Dot2 into complex128 (fields
+ * within ~1e-6 of the FP64 build; the mixed form's solve is 1e-6-accurate). */
 int egx_set_level_precision(egx_ctx *ctx, int precision);
 /* Impedance, apparent resistivity and phase at n sites from the total fields
  * of polarisation X (e1, h1) and Y (e2, h2), each [n][3] complex, host arrays
