@@ -101,6 +101,59 @@ __global__ void k_multi_dot(const C<T> *__restrict__ V, int ncols, const C<T> *_
     }
 }
 
+// complex64 vectors of even length: the same dots with each load a float4
+// (two complex entries), four per column and pass
+__global__ void k_multi_dot_c2(const float4 *__restrict__ V, int ncols, const float4 *__restrict__ w, long n2,
+                               double2 *__restrict__ partials) {
+    constexpr int ROWS = 4;
+    const long stride = (long)gridDim.x * blockDim.x;
+    auto fma_conj2 = [](float2 &acc, float4 a, float4 b) {  // += conj(a) b, two entries
+        acc.x = fmaf(a.x, b.x, acc.x);
+        acc.x = fmaf(a.y, b.y, acc.x);
+        acc.y = fmaf(a.x, b.y, acc.y);
+        acc.y = fmaf(-a.y, b.x, acc.y);
+        acc.x = fmaf(a.z, b.z, acc.x);
+        acc.x = fmaf(a.w, b.w, acc.x);
+        acc.y = fmaf(a.z, b.w, acc.y);
+        acc.y = fmaf(-a.w, b.z, acc.y);
+    };
+    for (int k0 = 0; k0 < ncols; k0 += kDotCols) {
+        const int kc = min(kDotCols, ncols - k0);
+        const float4 *col = V + (long)k0 * n2;
+        float2 acc[kDotCols];
+#pragma unroll
+        for (int j = 0; j < kDotCols; j++) acc[j] = make_float2(0.f, 0.f);
+        long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+        for (; r + (ROWS - 1) * stride < n2; r += ROWS * stride) {
+            float4 x[ROWS];
+#pragma unroll
+            for (int u = 0; u < ROWS; u++) x[u] = w[r + u * stride];
+#pragma unroll
+            for (int j = 0; j < kDotCols; j++)
+                if (j < kc) {
+                    float4 a[ROWS];
+#pragma unroll
+                    for (int u = 0; u < ROWS; u++) a[u] = col[(long)j * n2 + r + u * stride];
+#pragma unroll
+                    for (int u = 0; u < ROWS; u++) fma_conj2(acc[j], a[u], x[u]);
+                }
+        }
+        for (; r < n2; r += stride) {
+            const float4 x = w[r];
+#pragma unroll
+            for (int j = 0; j < kDotCols; j++)
+                if (j < kc) fma_conj2(acc[j], col[(long)j * n2 + r], x);
+        }
+#pragma unroll
+        for (int j = 0; j < kDotCols; j++) {
+            if (j < kc) {
+                double2 sm = block_sum2(make_double2((double)acc[j].x, (double)acc[j].y));
+                if (threadIdx.x == 0) partials[(long)blockIdx.x * ncols + k0 + j] = sm;
+            }
+        }
+    }
+}
+
 __global__ void k_reduce_cols(const double2 *__restrict__ partials, int nblocks, int ncols, double2 *__restrict__ out) {
     const int k = blockIdx.x;
     double2 s = make_double2(0, 0);
@@ -145,6 +198,39 @@ __global__ void k_update_norm(const C<T> *__restrict__ V, int ncols, const doubl
     }
     double s = block_sum((double)acc);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// complex64 vectors of even length: the update with float4 loads
+__global__ void k_update_norm_c2(const float4 *__restrict__ V, int ncols, const double2 *__restrict__ dots, float4 *w,
+                                 long n2, double *__restrict__ partials) {
+    __shared__ float2 sd[64];
+    for (int k = threadIdx.x; k < ncols; k += blockDim.x) sd[k] = make_float2((float)dots[k].x, (float)dots[k].y);
+    __syncthreads();
+    const long stride = (long)gridDim.x * blockDim.x;
+    float acc = 0.f;
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n2; r += stride) {
+        float4 v = w[r];
+#pragma unroll 4
+        for (int k = 0; k < ncols; k++) {
+            const float4 a = V[(long)k * n2 + r];
+            const float2 d = sd[k];
+            v.x = fmaf(-a.x, d.x, v.x);
+            v.x = fmaf(a.y, d.y, v.x);
+            v.y = fmaf(-a.x, d.y, v.y);
+            v.y = fmaf(-a.y, d.x, v.y);
+            v.z = fmaf(-a.z, d.x, v.z);
+            v.z = fmaf(a.w, d.y, v.z);
+            v.w = fmaf(-a.z, d.y, v.w);
+            v.w = fmaf(-a.w, d.x, v.w);
+        }
+        w[r] = v;
+        acc = fmaf(v.x, v.x, acc);
+        acc = fmaf(v.y, v.y, acc);
+        acc = fmaf(v.z, v.z, acc);
+        acc = fmaf(v.w, v.w, acc);
+    }
+    double sm = block_sum((double)acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = sm;
 }
 
 template <typename T>
@@ -216,13 +302,21 @@ static int grid_for(long n) {
 template <typename T>
 void VecOps<T>::multi_dot(const C<T> *V, int ncols, const C<T> *w, long n, double2 *dots_dev, double2 *partials,
                           int nblocks, cudaStream_t s) {
-    k_multi_dot<T><<<nblocks, kThreads, 0, s>>>(V, ncols, w, n, partials);
+    if (sizeof(T) == sizeof(float) && n % 2 == 0)
+        k_multi_dot_c2<<<nblocks, kThreads, 0, s>>>(reinterpret_cast<const float4 *>(V), ncols,
+                                                    reinterpret_cast<const float4 *>(w), n / 2, partials);
+    else
+        k_multi_dot<T><<<nblocks, kThreads, 0, s>>>(V, ncols, w, n, partials);
     k_reduce_cols<<<ncols, kThreads, 0, s>>>(partials, nblocks, ncols, dots_dev);
 }
 template <typename T>
 void VecOps<T>::update_norm(const C<T> *V, int ncols, const double2 *dots_dev, C<T> *w, long n, double *norm2_dev,
                             double *partials, int nblocks, cudaStream_t s) {
-    k_update_norm<T><<<nblocks, kThreads, 0, s>>>(V, ncols, dots_dev, w, n, partials);
+    if (sizeof(T) == sizeof(float) && n % 2 == 0)
+        k_update_norm_c2<<<nblocks, kThreads, 0, s>>>(reinterpret_cast<const float4 *>(V), ncols, dots_dev,
+                                                      reinterpret_cast<float4 *>(w), n / 2, partials);
+    else
+        k_update_norm<T><<<nblocks, kThreads, 0, s>>>(V, ncols, dots_dev, w, n, partials);
     k_reduce_scalar<<<1, kThreads, 0, s>>>(partials, nblocks, norm2_dev);
 }
 template <typename T>
