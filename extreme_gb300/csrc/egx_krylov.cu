@@ -102,10 +102,11 @@ __global__ void k_multi_dot(const C<T> *__restrict__ V, int ncols, const C<T> *_
 }
 
 // complex64 vectors of even length: the same dots with each load a float4
-// (two complex entries), four per column and pass
+// (two complex entries), four per column and pass, eight columns per pass
+// (66 registers: three CTAs per SM where sixteen columns allowed two)
 __global__ void k_multi_dot_c2(const float4 *__restrict__ V, int ncols, const float4 *__restrict__ w, long n2,
                                double2 *__restrict__ partials) {
-    constexpr int ROWS = 4;
+    constexpr int ROWS = 4, kDotCols = 8;
     const long stride = (long)gridDim.x * blockDim.x;
     auto fma_conj2 = [](float2 &acc, float4 a, float4 b) {  // += conj(a) b, two entries
         acc.x = fmaf(a.x, b.x, acc.x);
