@@ -41,18 +41,31 @@ template <> struct RegFft<512> { static constexpr int R1 = 8, R2 = 8, R3 = 8; };
 
 inline bool reg_fft_ok(int n) { return n == 64 || n == 128 || n == 256 || n == 512; }
 
-// columns per CTA: 128-byte rows
-template <typename T> struct RegCols { static constexpr int BT = 128 / (int)sizeof(C<T>); };
+// columns per CTA: 128-byte rows (BT), or 64-byte rows (BTN: twice the CTAs
+// of half the size, which overlap their load, exchange and store phases
+// better where the pass is latency-bound)
+template <typename T> struct RegCols {
+    static constexpr int BT = 128 / (int)sizeof(C<T>);
+    static constexpr int BTN = 64 / (int)sizeof(C<T>);
+};
 
-template <int N, typename T> constexpr int reg_threads() { return N / RegFft<N>::R1 * RegCols<T>::BT; }
+template <int N, typename T, int BT = RegCols<T>::BT> constexpr int reg_threads() { return N / RegFft<N>::R1 * BT; }
 
-template <int N, typename T> constexpr size_t reg_smem() { return (size_t)N * RegCols<T>::BT * sizeof(C<T>); }
+template <int N, typename T, int BT = RegCols<T>::BT> constexpr size_t reg_smem() {
+    return (size_t)N * BT * sizeof(C<T>);
+}
+
+// resident CTAs per SM the latency-bound y passes are compiled for: a full
+// SM of threads, at most four CTAs
+template <int N, typename T, int BT = RegCols<T>::BT> constexpr int reg_min_blocks() {
+    return 2048 / reg_threads<N, T, BT>() < 4 ? 2048 / reg_threads<N, T, BT>() : 4;
+}
 
 // load(n) -> C<T> (element n of this thread's column), store(k, v)
-template <typename T, int N, class Load, class Store>
+template <typename T, int N, int BT = RegCols<T>::BT, class Load, class Store>
 __device__ __forceinline__ void fft_reg(C<T> *S, const C<T> *__restrict__ tw, int sign, Load load, Store store) {
     constexpr int R1 = RegFft<N>::R1, R2 = RegFft<N>::R2, R3 = RegFft<N>::R3;
-    constexpr int M = R2 * R3, TPC = N / R1, BT = RegCols<T>::BT;
+    constexpr int M = R2 * R3, TPC = N / R1;
     static_assert(R1 == R2 && R3 <= R1 && R1 * R2 * R3 == N, "radix plan");
     const int c = threadIdx.x % BT, u = threadIdx.x / BT;
     // pass 1: thread m = u

@@ -125,16 +125,18 @@ __global__ void k_bwd_y(const C<T> *__restrict__ buf, const C<T> *__restrict__ x
 // ------------------------------------------------------------------
 // The same three steps on the register-resident DFT (egx_fft_reg.cuh) for
 // lengths in {64, 128, 256, 512}: one CTA per line and 128-byte tile of
-// columns, every global access a whole 128-byte row segment. The y passes
-// are latency-bound on their global loads: they are compiled for two CTAs
-// per SM (at 1,024 threads per CTA that is 32 registers and a few spilled
-// words, which measured faster than one CTA with 48 registers).
-template <typename T, int N>
-__global__ void __launch_bounds__(reg_threads<N, T>(), 2)
+// columns, every global access a whole row segment of BT columns. The y
+// passes and the forward x pass run 64-byte tiles (512 threads per CTA for
+// complex64, four CTAs per SM at 32 registers), whose CTAs overlap their
+// load, exchange and store phases better than two 1,024-thread CTAs of
+// 128-byte tiles (fwd y 0.174 -> 0.146 ms, fwd x 0.240 -> 0.227 ms at
+// 256x256x48, two sources); the backward x pass keeps 128-byte tiles
+// (0.211 ms, 0.248 with 64-byte tiles).
+template <typename T, int N, int BT>
+__global__ void __launch_bounds__(reg_threads<N, T, BT>(), reg_min_blocks<N, T, BT>())
     k_fwd_y_r(const C<T> *__restrict__ x, const OperatorData<T> op, C<T> *__restrict__ buf, const OpDims d,
               const C<T> *__restrict__ tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int BT = RegCols<T>::BT;
     const int i = blockIdx.x;
     const int b = blockIdx.y * BT + (int)(threadIdx.x % BT);
     const bool bok = b < d.B;
@@ -150,15 +152,14 @@ __global__ void __launch_bounds__(reg_threads<N, T>(), 2)
     auto store = [&](int j, C<T> v) {
         if (bok) buf[((long)i * N + j) * d.B + b] = v;
     };
-    fft_reg<T, N>(reinterpret_cast<C<T> *>(smem_raw), tw, -1, load, store);
+    fft_reg<T, N, BT>(reinterpret_cast<C<T> *>(smem_raw), tw, -1, load, store);
 }
 
-template <typename T, int N>
-__global__ void __launch_bounds__(reg_threads<N, T>())
+template <typename T, int N, int BT>
+__global__ void __launch_bounds__(reg_threads<N, T, BT>())
     k_lines_r(C<T> *buf, long lstride, long estride, int B, int nload, int nstore, const C<T> *__restrict__ tw,
               int sign) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int BT = RegCols<T>::BT;
     const int b = blockIdx.y * BT + (int)(threadIdx.x % BT);
     const bool bok = b < B;
     C<T> *line = buf + (long)blockIdx.x * lstride + b;
@@ -166,15 +167,14 @@ __global__ void __launch_bounds__(reg_threads<N, T>())
     auto store = [&](int e, C<T> v) {
         if (bok && e < nstore) line[e * estride] = v;
     };
-    fft_reg<T, N>(reinterpret_cast<C<T> *>(smem_raw), tw, sign, load, store);
+    fft_reg<T, N, BT>(reinterpret_cast<C<T> *>(smem_raw), tw, sign, load, store);
 }
 
-template <typename T, int N>
-__global__ void __launch_bounds__(reg_threads<N, T>(), 2)
+template <typename T, int N, int BT>
+__global__ void __launch_bounds__(reg_threads<N, T, BT>(), reg_min_blocks<N, T, BT>())
     k_bwd_y_r(const C<T> *__restrict__ buf, const C<T> *__restrict__ x, const OperatorData<T> op,
               C<T> *__restrict__ y, const OpDims d, const C<T> *__restrict__ tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int BT = RegCols<T>::BT;
     const int i = blockIdx.x;
     const int b = blockIdx.y * BT + (int)(threadIdx.x % BT);
     const bool bok = b < d.B;
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(reg_threads<N, T>(), 2)
         const C<T> rx = cmul<T>(op.r[cell * d.nz + k], xv);
         y[idx] = (op.type == EGX_OP_A) ? csub<T>(csub<T>(xv, yv), rx) : cadd<T>(yv, rx);
     };
-    fft_reg<T, N>(reinterpret_cast<C<T> *>(smem_raw), tw, +1, load, store);
+    fft_reg<T, N, BT>(reinterpret_cast<C<T> *>(smem_raw), tw, +1, load, store);
 }
 
 // Lines whose second half is the parity image of the first: element e of a
@@ -219,29 +219,44 @@ __global__ void __launch_bounds__(reg_threads<N, T>())
     fft_reg<T, N>(reinterpret_cast<C<T> *>(smem_raw), tw, sign, load, store);
 }
 
-template <typename T, int N>
+template <typename T, int N, int BT = RegCols<T>::BT>
 static void reg_attr(const void *fn) {
-    constexpr size_t sm = reg_smem<N, T>();
+    constexpr size_t sm = reg_smem<N, T, BT>();
     raise_smem_limit(fn, sm);
 }
 
 // which: 0 fwd_y, 1 lines, 2 bwd_y
-template <typename T, int N>
-static void launch_reg(int which, dim3 grid, cudaStream_t s, const C<T> *x, const OperatorData<T> *op, C<T> *buf,
+template <typename T, int N, int BT>
+static void launch_reg(int which, cudaStream_t s, int nlines, const C<T> *x, const OperatorData<T> *op, C<T> *buf,
                        C<T> *y, const OpDims *d, long lstride, long estride, int B, int nload, int nstore,
                        const C<T> *tw, int sign) {
-    constexpr size_t sm = reg_smem<N, T>();
-    constexpr int thr = reg_threads<N, T>();
+    constexpr size_t sm = reg_smem<N, T, BT>();
+    constexpr int thr = reg_threads<N, T, BT>();
+    const dim3 grid(nlines, (B + BT - 1) / BT);
     if (which == 0) {
-        reg_attr<T, N>((const void *)k_fwd_y_r<T, N>);
-        k_fwd_y_r<T, N><<<grid, thr, sm, s>>>(x, *op, buf, *d, tw);
+        reg_attr<T, N, BT>((const void *)k_fwd_y_r<T, N, BT>);
+        k_fwd_y_r<T, N, BT><<<grid, thr, sm, s>>>(x, *op, buf, *d, tw);
     } else if (which == 1) {
-        reg_attr<T, N>((const void *)k_lines_r<T, N>);
-        k_lines_r<T, N><<<grid, thr, sm, s>>>(buf, lstride, estride, B, nload, nstore, tw, sign);
+        reg_attr<T, N, BT>((const void *)k_lines_r<T, N, BT>);
+        k_lines_r<T, N, BT><<<grid, thr, sm, s>>>(buf, lstride, estride, B, nload, nstore, tw, sign);
     } else {
-        reg_attr<T, N>((const void *)k_bwd_y_r<T, N>);
-        k_bwd_y_r<T, N><<<grid, thr, sm, s>>>(buf, x, *op, y, *d, tw);
+        reg_attr<T, N, BT>((const void *)k_bwd_y_r<T, N, BT>);
+        k_bwd_y_r<T, N, BT><<<grid, thr, sm, s>>>(buf, x, *op, y, *d, tw);
     }
+}
+
+template <typename T, int N>
+static void launch_reg_tile(int which, cudaStream_t s, int nlines, const C<T> *x, const OperatorData<T> *op,
+                            C<T> *buf, C<T> *y, const OpDims *d, long lstride, long estride, int B, int nload,
+                            int nstore, const C<T> *tw, int sign) {
+    // 64-byte tiles for the y passes and for x passes that write more rows
+    // than they read; 128-byte tiles otherwise
+    if (which != 1 || nload < nstore)
+        launch_reg<T, N, RegCols<T>::BTN>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw,
+                                           sign);
+    else
+        launch_reg<T, N, RegCols<T>::BT>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw,
+                                          sign);
 }
 
 // returns false when n has no register plan
@@ -250,13 +265,11 @@ static bool run_reg(int n, int which, int nlines, int B, cudaStream_t s, const C
                     C<T> *buf, C<T> *y, const OpDims *d, long lstride, long estride, int nload, int nstore,
                     const C<T> *tw, int sign) {
     if (!reg_fft_ok(n)) return false;
-    constexpr int BT = RegCols<T>::BT;
-    dim3 grid(nlines, (B + BT - 1) / BT);
     switch (n) {
-        case 64: launch_reg<T, 64>(which, grid, s, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
-        case 128: launch_reg<T, 128>(which, grid, s, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
-        case 256: launch_reg<T, 256>(which, grid, s, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
-        default: launch_reg<T, 512>(which, grid, s, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
+        case 64: launch_reg_tile<T, 64>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
+        case 128: launch_reg_tile<T, 128>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
+        case 256: launch_reg_tile<T, 256>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
+        default: launch_reg_tile<T, 512>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
     }
     return true;
 }
