@@ -263,7 +263,10 @@ def run_ours(args, rank, world, local):
     barrier()
     sampler = ClockSampler(local)
     sampler.start()
-    ctx.profile(True)
+    # only the contraction is timed by events inside the timed region (the
+    # roofline's per-launch time); the per-kernel table comes from a second,
+    # profiled pass over the same steps below
+    ctx.profile(True, kinds=[egx.K_CONTRACT + egx.K_C64])
     l0 = ctx.launch_count()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     results = []
@@ -277,6 +280,11 @@ def run_ours(args, rank, world, local):
     clocks = sampler.stop()
     launches = ctx.launch_count() - l0
     kc, kms = ctx.profile_read(egx.K_CONTRACT + egx.K_C64)
+    # ---- per-kernel table: the same steps again with every kind timed
+    ctx.profile(True)
+    for i in range(args.steps):
+        step(i, egx.DEVICE)
+    torch.cuda.synchronize(dev)
     kernels = {}
     for k, name in egx.KERNEL_NAMES.items():
         for off, tag in ((0, ""), (egx.K_C64, "_c64")):
@@ -374,6 +382,7 @@ def run_ours(args, rank, world, local):
         "gpu_launches": launches,
         "launches_before_timed": l0,
         "kernels": kernels,
+        "kernels_source": "a second pass over the same steps after the timed region, every kernel kind event-timed",
         "step_ms": [round(t, 1) for t in step_ms],
         "solves": [[{k: r[k] for k in ("converged", "iterations", "n_applies", "n_refinements", "true_be")}
                     for r in res] for res in results],

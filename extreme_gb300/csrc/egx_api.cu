@@ -523,6 +523,12 @@ int egx_profile(egx_ctx *ctx, int enable) {
     });
 }
 
+int egx_profile_kinds(egx_ctx *ctx, unsigned mask) {
+    if (!ctx) return EGX_ERR_INVALID;
+    ctx->timers.mask = mask;
+    return EGX_OK;
+}
+
 int egx_profile_read(egx_ctx *ctx, int kind, long *launches, double *total_ms) {
     if (!ctx || !launches || !total_ms || kind < 0 || kind >= Timers::kKinds) return EGX_ERR_INVALID;
     EGX_GUARD(ctx, {

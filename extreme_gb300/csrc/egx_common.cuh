@@ -80,6 +80,7 @@ struct Error : std::runtime_error {
 struct Timers {
     static const int kKinds = 32;
     bool on = false;
+    unsigned mask = ~0u;  // kinds recorded while on
     struct Rec {
         int kind;
         cudaEvent_t a, b;
@@ -100,7 +101,7 @@ struct Timers {
     }
     // returns the record index to close with end()
     int begin(int kind, cudaStream_t s) {
-        if (!on) return -1;
+        if (!on || kind < 0 || kind >= kKinds || !((mask >> kind) & 1u)) return -1;
         Rec r{kind, take(), take()};
         cudaEventRecord(r.a, s);
         pending.push_back(r);

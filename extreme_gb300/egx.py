@@ -25,7 +25,8 @@ EXPORTS = [
     "egx_green_build", "egx_green_upload", "egx_green_download", "egx_green_free",
     "egx_op_prepare", "egx_op_apply", "egx_op_apply_ds", "egx_op_apply_c64", "egx_fft2d",
     "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products", "egx_dot_products_static",
-    "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_read",
+    "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_kinds",
+    "egx_profile_read",
     "egx_level_fields", "egx_level_cache", "egx_set_level_precision", "egx_mt_responses", "egx_wait_selftest",
     "egx_net_create", "egx_net_free", "egx_net_size", "egx_net_params", "egx_net_set_model", "egx_net_loss_grad",
     "egx_net_adam", "egx_net_apply", "egx_learned_stats",
@@ -131,6 +132,7 @@ def load(path=None):
     lib.egx_net_apply.argtypes = [vp, vp, vp, vp, i, i]
     lib.egx_learned_stats.argtypes = [vp, C.POINTER(C.c_long), C.POINTER(C.c_long)]
     lib.egx_profile.argtypes = [vp, i]
+    lib.egx_profile_kinds.argtypes = [vp, C.c_uint]
     lib.egx_profile_read.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_double)]
     _lib = lib
     return lib
@@ -376,7 +378,10 @@ class Context:
                                               C.c_void_p(jq_ptr), nsrc, C.c_void_p(e_ptr), C.c_void_p(h_ptr),
                                               DEVICE))
 
-    def profile(self, enable=True):
+    def profile(self, enable=True, kinds=None):
+        """Per-kernel event timing on (the kinds listed, default all) or off."""
+        mask = 0xFFFFFFFF if kinds is None else sum(1 << k for k in kinds)
+        self._check(self.lib.egx_profile_kinds(self.h, mask))
         self._check(self.lib.egx_profile(self.h, int(enable)))
 
     def profile_read(self, kind):

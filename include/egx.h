@@ -302,8 +302,12 @@ enum {
     EGX_K_GREEN_LAYERS = 16, EGX_K_GREEN_KERNELS = 17, EGX_K_GREEN_HANKEL = 18, EGX_K_GREEN_CELLS = 19,
     EGX_K_GREEN_FFT = 20
 };
-/* enable != 0 records CUDA events around every instrumented launch. */
+/* enable != 0 records CUDA events around every instrumented launch (of the
+ * kinds selected by egx_profile_kinds); resets the sums. */
 int egx_profile(egx_ctx *ctx, int enable);
+/* Bit k of mask selects kind k (default: all); fewer kinds, fewer event
+ * records on the host's path between launches. */
+int egx_profile_kinds(egx_ctx *ctx, unsigned mask);
 /* Launches and summed device milliseconds of one kernel kind since enable. */
 int egx_profile_read(egx_ctx *ctx, int kind, long *launches, double *total_ms);
 
