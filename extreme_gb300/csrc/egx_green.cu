@@ -171,36 +171,55 @@ __global__ void k_kernels(const double *__restrict__ lam, int nl, const double2 
         return dadd(acc, dscal(c3, v3));
     };
     auto lin2 = [](double c1, double2 v1, double c2, double2 v2) { return dadd(dscal(c1, v1), dscal(c2, v2)); };
-    // CalculateT / CalculateR
-    double2 Tt = dexp(lin3(-r1, er, -s1, es, 2 * dt, et));
-    Tt = dsub(Tt, dexp(lin3(-r1, er, -s2, es, 2 * dt, et)));
-    Tt = dsub(Tt, dexp(lin3(-r2, er, -s1, es, 2 * dt, et)));
-    Tt = dadd(Tt, dexp(lin3(-r2, er, -s2, es, 2 * dt, et)));
-    double2 Rr = dexp(lin3(-2 * db1, eb, s2, es, r2, er));
-    Rr = dsub(Rr, dexp(lin3(-2 * db1, eb, s1, es, r2, er)));
-    Rr = dsub(Rr, dexp(lin3(-2 * db1, eb, s2, es, r1, er)));
-    Rr = dadd(Rr, dexp(lin3(-2 * db1, eb, s1, es, r1, er)));
-    double2 C = dmk(0, 0), D = dmk(0, 0);
-    if (T0.kase == 2) {  // receiver above: CTop, DTop
-        C = dexp(lin2(-s1, es, r2, er));
-        C = dsub(C, dexp(lin2(-s2, es, r2, er)));
-        C = dsub(C, dexp(lin2(-s1, es, r1, er)));
-        C = dadd(C, dexp(lin2(-s2, es, r1, er)));
-        double2 F = lin2(-2 * db1, eb, 2 * dt, et);
-        D = dexp(dadd(dadd(F, dscal(s2, es)), dscal(-r1, er)));
-        D = dsub(D, dexp(dadd(dadd(F, dscal(s1, es)), dscal(-r1, er))));
-        D = dsub(D, dexp(dadd(dadd(F, dscal(s2, es)), dscal(-r2, er))));
-        D = dadd(D, dexp(dadd(dadd(F, dscal(s1, es)), dscal(-r2, er))));
-    } else if (T0.kase == 1) {  // receiver below: CBot, DBot
-        C = dexp(lin2(-r1, er, s2, es));
-        C = dsub(C, dexp(lin2(-r1, er, s1, es)));
-        C = dsub(C, dexp(lin2(-r2, er, s2, es)));
-        C = dadd(C, dexp(lin2(-r2, er, s1, es)));
-        double2 F = lin2(-2 * db1, eb, 2 * dt, et);
-        D = dexp(dadd(dadd(F, dscal(-s1, es)), dscal(r2, er)));
-        D = dsub(D, dexp(dadd(dadd(F, dscal(-s2, es)), dscal(r2, er))));
-        D = dsub(D, dexp(dadd(dadd(F, dscal(-s1, es)), dscal(r1, er))));
-        D = dadd(D, dexp(dadd(dadd(F, dscal(-s2, es)), dscal(r1, er))));
+    // CalculateT / CalculateR and the C, D sums. Each is a signed sum of four
+    // exponentials of the form e^G (e^a - e^b)(e^c - e^d) over the receiver
+    // interval [r1, r2] and the source interval [s1, s2], so it equals its
+    // first term times fr fs, fr = 1 - e^{-(r2 - r1) er}, fs = 1 - e^{-(s2 - s1) es}:
+    // six complex exponentials instead of sixteen. With r1 <= r2, s1 <= s2
+    // and Re eta >= 0 the factors have modulus <= 2 and the leading exponent
+    // is the four-term form's first one, so nothing overflows that did not.
+    double2 Tt, Rr, C = dmk(0, 0), D = dmk(0, 0);
+    const double2 F = lin2(-2 * db1, eb, 2 * dt, et);
+    if (r1 <= r2 && s1 <= s2) {
+        const double2 fsr = dmul(dsub(dmk(1, 0), dexp(dscal(-(r2 - r1), er))),
+                                 dsub(dmk(1, 0), dexp(dscal(-(s2 - s1), es))));
+        Tt = dmul(dexp(lin3(-r1, er, -s1, es, 2 * dt, et)), fsr);
+        Rr = dmul(dexp(lin3(-2 * db1, eb, s2, es, r2, er)), fsr);
+        if (T0.kase == 2) {  // receiver above: CTop, DTop
+            C = dmul(dexp(lin2(-s1, es, r2, er)), fsr);
+            D = dmul(dexp(dadd(dadd(F, dscal(s2, es)), dscal(-r1, er))), fsr);
+        } else if (T0.kase == 1) {  // receiver below: CBot, DBot
+            C = dmul(dexp(lin2(-r1, er, s2, es)), fsr);
+            D = dmul(dexp(dadd(dadd(F, dscal(-s1, es)), dscal(r2, er))), fsr);
+        }
+    } else {
+        Tt = dexp(lin3(-r1, er, -s1, es, 2 * dt, et));
+        Tt = dsub(Tt, dexp(lin3(-r1, er, -s2, es, 2 * dt, et)));
+        Tt = dsub(Tt, dexp(lin3(-r2, er, -s1, es, 2 * dt, et)));
+        Tt = dadd(Tt, dexp(lin3(-r2, er, -s2, es, 2 * dt, et)));
+        Rr = dexp(lin3(-2 * db1, eb, s2, es, r2, er));
+        Rr = dsub(Rr, dexp(lin3(-2 * db1, eb, s1, es, r2, er)));
+        Rr = dsub(Rr, dexp(lin3(-2 * db1, eb, s2, es, r1, er)));
+        Rr = dadd(Rr, dexp(lin3(-2 * db1, eb, s1, es, r1, er)));
+        if (T0.kase == 2) {
+            C = dexp(lin2(-s1, es, r2, er));
+            C = dsub(C, dexp(lin2(-s2, es, r2, er)));
+            C = dsub(C, dexp(lin2(-s1, es, r1, er)));
+            C = dadd(C, dexp(lin2(-s2, es, r1, er)));
+            D = dexp(dadd(dadd(F, dscal(s2, es)), dscal(-r1, er)));
+            D = dsub(D, dexp(dadd(dadd(F, dscal(s1, es)), dscal(-r1, er))));
+            D = dsub(D, dexp(dadd(dadd(F, dscal(s2, es)), dscal(-r2, er))));
+            D = dadd(D, dexp(dadd(dadd(F, dscal(s1, es)), dscal(-r2, er))));
+        } else if (T0.kase == 1) {
+            C = dexp(lin2(-r1, er, s2, es));
+            C = dsub(C, dexp(lin2(-r1, er, s1, es)));
+            C = dsub(C, dexp(lin2(-r2, er, s2, es)));
+            C = dadd(C, dexp(lin2(-r2, er, s1, es)));
+            D = dexp(dadd(dadd(F, dscal(-s1, es)), dscal(r2, er)));
+            D = dsub(D, dexp(dadd(dadd(F, dscal(-s2, es)), dscal(r2, er))));
+            D = dsub(D, dexp(dadd(dadd(F, dscal(-s1, es)), dscal(r1, er))));
+            D = dadd(D, dexp(dadd(dadd(F, dscal(-s2, es)), dscal(r1, er))));
+        }
     }
     // propagator chain A[t, b] of a mode
     auto chain = [&](const double2 *P, const double2 *Q) {
