@@ -82,7 +82,8 @@ struct LayerArgs {
     double tops[kMaxLayers + 1];
 };
 
-// Per lambda: eta, exp, P1, Q1, Ps, Qs over all layers. Arrays [6][L][nl].
+// Per lambda: eta, exp, P1, Q1, Ps, Qs over all layers. Arrays [6][L][nl]
+// (of the ten that k_chain_factors completes).
 __global__ void k_layers(const double *__restrict__ lam, int nl, const LayerArgs a, double2 *__restrict__ out) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nl) return;
@@ -144,6 +145,33 @@ struct Trans {
     int r, s;      // background layers of receiver / transmitter
     int kase;      // 0 match, 1 receiver below, 2 receiver above
 };
+
+// The propagator chains' per-layer pieces, which depend on the layer and
+// lambda only (not on the transmitter pair): per mode (P1/Q1, Ps/Qs) the
+// head H[b] = 1 / (eta_b (1 - P_b Q_b X_b)) and the factors
+// F[k] = (1 + P_{k+1}) / (1 + P_k X_k) exp(z_{k+1} (eta_{k+1} - eta_k)),
+// so that a pair's chain A[t, b] = F[t] (... (F[b-1] H[b])) is a few complex
+// products. Arrays [mode][L][nl] after the six of k_layers: F at 6L nl, H at
+// 8L nl.
+__global__ void k_chain_factors(int nl, const LayerArgs a, double2 *__restrict__ lay) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nl) return;
+    const int L = a.L;
+    const double2 *Eta = lay, *Ex = lay + (long)L * nl;
+    auto E = [&](int k) { return Eta[(long)k * nl + m]; };
+    for (int mode = 0; mode < 2; mode++) {
+        const double2 *P = lay + (2L + 2 * mode) * L * nl, *Q = lay + (3L + 2 * mode) * L * nl;
+        double2 *F = lay + (6L + mode) * L * nl, *H = lay + (8L + mode) * L * nl;
+        for (int b = 0; b < L; b++)
+            H[(long)b * nl + m] = drecip(dmul(E(b), dsub(dmk(1, 0), dmul(dmul(P[(long)b * nl + m], Q[(long)b * nl + m]),
+                                                                       Ex[(long)b * nl + m]))));
+        for (int k = 0; k + 1 < L; k++) {
+            const double2 num = dadd(dmk(1, 0), P[(long)(k + 1) * nl + m]);
+            const double2 den = dadd(dmk(1, 0), dmul(P[(long)k * nl + m], Ex[(long)k * nl + m]));
+            F[(long)k * nl + m] = dmul(ddiv(num, den), dexp(dscal(a.tops[k + 1], dsub(E(k + 1), E(k)))));
+        }
+    }
+}
 
 // which kernels: bit0 U1, bit1 U2, bit2 U3, bit3 U4, bit4 U5; outputs packed
 // in that order, each [ntrans][nl_total] at column offset `col0`.
@@ -221,15 +249,12 @@ __global__ void k_kernels(const double *__restrict__ lam, int nl, const double2 
             D = dadd(D, dexp(dadd(dadd(F, dscal(-s2, es)), dscal(r1, er))));
         }
     }
-    // propagator chain A[t, b] of a mode
-    auto chain = [&](const double2 *P, const double2 *Q) {
-        double2 A = drecip(dmul(E(b), dsub(dmk(1, 0), dmul(dmul(P[(long)b * nl + m], Q[(long)b * nl + m]), X(b)))));
-        for (int k = b - 1; k >= t; k--) {
-            double2 num = dadd(dmk(1, 0), P[(long)(k + 1) * nl + m]);
-            double2 den = dadd(dmk(1, 0), dmul(P[(long)k * nl + m], X(k)));
-            double2 f = dmul(ddiv(num, den), dexp(dscal(a.tops[k + 1], dsub(E(k + 1), E(k)))));
-            A = dmul(f, A);
-        }
+    // propagator chain A[t, b] of a mode from the per-layer pieces of
+    // k_chain_factors
+    auto chain = [&](int mode) {
+        const double2 *F = lay + (6L + mode) * L * nl, *H = lay + (8L + mode) * L * nl;
+        double2 A = H[(long)b * nl + m];
+        for (int k = b - 1; k >= t; k--) A = dmul(F[(long)k * nl + m], A);
         return A;
     };
     auto psi1 = [&](const double2 *P, const double2 *Q) {
@@ -265,12 +290,12 @@ __global__ void k_kernels(const double *__restrict__ lam, int nl, const double2 
     double2 *Ub = U + (long)tr * nl_total + col0 + m;
     const long ustride = (long)ntrans * nl_total;
     if (which & 1) {
-        double2 ann = chain(P1, Q1);
+        double2 ann = chain(0);
         double2 u = dmul(dmul(ann, annf), special(P1, Q1, 1, 1, psi1(P1, Q1)));
         u = dmul(u, dmk(0.0, a.omega * kMu0 * 0.5));
         Ub[ustride * out++] = u;
     }
-    double2 anns = chain(Ps, Qs);
+    double2 anns = chain(1);
     if (r > s) anns = dmul(ddiv(a.zeta[r], a.zeta[s]), anns);
     if (which & 2) {
         double2 u = dmul(anns, special(Ps, Qs, 1, -1, psi1(Ps, Qs)));
@@ -807,19 +832,15 @@ __global__ void k_kernels_vtp(const double *__restrict__ lam, int nl, const doub
     const int r = T0.r, s = T0.s, t = min(r, s), b = max(r, s);
     const double l = lam[m];
     auto E = [&](int k) { return Eta[(long)k * nl + m]; };
-    auto chain = [&](const double2 *P, const double2 *Q) {
-        double2 A = drecip(dmul(E(b), dsub(dmk(1, 0), dmul(dmul(P[(long)b * nl + m], Q[(long)b * nl + m]),
-                                                             Ex[(long)b * nl + m]))));
-        for (int k = b - 1; k >= t; k--) {
-            double2 num = dadd(dmk(1, 0), P[(long)(k + 1) * nl + m]);
-            double2 den = dadd(dmk(1, 0), dmul(P[(long)k * nl + m], Ex[(long)k * nl + m]));
-            A = dmul(dmul(ddiv(num, den), dexp(dscal(a.tops[k + 1], dsub(E(k + 1), E(k))))), A);
-        }
+    auto chain = [&](int mode) {  // k_chain_factors' pieces, as in k_kernels
+        const double2 *F = lay + (6L + mode) * L * nl, *H = lay + (8L + mode) * L * nl;
+        double2 A = H[(long)b * nl + m];
+        for (int k = b - 1; k >= t; k--) A = dmul(F[(long)k * nl + m], A);
         return A;
     };
     const double2 er = E(r), es = E(s);
-    const double2 a1 = chain(P1, Q1);
-    double2 as = chain(Ps, Qs);
+    const double2 a1 = chain(0);
+    double2 as = chain(1);
     if (r > s) as = dmul(ddiv(a.zeta[r], a.zeta[s]), as);
     const VtpTerms v1 = vtp_terms(Eta, P1, Q1, nl, m, a, T0, l);
     const VtpTerms vs = vtp_terms(Eta, Ps, Qs, nl, m, a, T0, l);
@@ -1257,9 +1278,11 @@ void build_green(const GreenModel &m, int n_hankels, cudaStream_t s, DevBuf &qua
         for (size_t it = 0; it < items.size(); it++) {
             const int nl = (int)lams[it].size();
             double *dl = dev_upload(d_lam, lams[it], s);
-            d_lay.ensure((size_t)6 * L * nl * sizeof(double2));
+            d_lay.ensure((size_t)10 * L * nl * sizeof(double2));
             int ev = tm ? tm->begin(EGX_K_GREEN_LAYERS, s) : -1;
             k_layers<<<(nl + 127) / 128, 128, 0, s>>>(dl, nl, la, d_lay.as<double2>());
+            k_chain_factors<<<(nl + 127) / 128, 128, 0, s>>>(nl, la, d_lay.as<double2>());
+            if (launches) *launches += 1;
             if (tm) tm->end(ev, s);
             long nthreads = (long)ntrans * nl;
             ev = tm ? tm->begin(EGX_K_GREEN_KERNELS, s) : -1;
@@ -1502,8 +1525,10 @@ void build_level_green(const GreenModel &m, int n_hankels, double z, double shx,
     for (size_t it = 0; it < items.size(); it++) {
         const int nl = (int)lams[it].size();
         double *dl = dev_upload(w.d_lam, lams[it], s);
-        w.d_lay.ensure((size_t)6 * L * nl * sizeof(double2));
+        w.d_lay.ensure((size_t)10 * L * nl * sizeof(double2));
         k_layers<<<(nl + 127) / 128, 128, 0, s>>>(dl, nl, la, w.d_lay.as<double2>());
+        k_chain_factors<<<(nl + 127) / 128, 128, 0, s>>>(nl, la, w.d_lay.as<double2>());
+        if (launches) *launches += 1;
         const long nthreads = (long)ntrans * nl;
         k_kernels_vtp<<<(unsigned)((nthreads + 127) / 128), 128, 0, s>>>(
             dl, nl, w.d_lay.as<double2>(), la, dtrans, ntrans, kind, w.d_U.as<double2>(), nl_total, col0[it]);
