@@ -184,10 +184,9 @@ __global__ void k_kernels(const double *__restrict__ lam, int nl, const double2 
     const int m = (int)(idx - (long)tr * nl);
     const Trans T0 = trans[tr];
     const int L = a.L;
-    const double2 *Eta = lay, *Ex = lay + (long)L * nl, *P1 = lay + 2L * L * nl, *Q1 = lay + 3L * L * nl;
+    const double2 *Eta = lay, *P1 = lay + 2L * L * nl, *Q1 = lay + 3L * L * nl;
     const double2 *Ps = lay + 4L * L * nl, *Qs = lay + 5L * L * nl;
 #define E(k) Eta[(long)(k) * nl + m]
-#define X(k) Ex[(long)(k) * nl + m]
     const int r = T0.r, s = T0.s, t = min(r, s), b = max(r, s);
     const double dt = a.tops[t], db1 = a.tops[b + 1];
     const double r1 = T0.r1, r2 = T0.r2, s1 = T0.s1, s2 = T0.s2;
@@ -331,7 +330,6 @@ __global__ void k_kernels(const double *__restrict__ lam, int nl, const double2 
         Ub[ustride * out++] = dmul(u, ddiv(dmk(l * l, 0), zr2));
     }
 #undef E
-#undef X
 }
 
 // I[u][trans][g] = norm * sum_j h[430 - j] * U[u][trans][col0 + i + j]
@@ -400,9 +398,6 @@ struct Term {
 
 template <typename O> __device__ __forceinline__ O cell_out(double2 v);
 template <> __device__ __forceinline__ double2 cell_out<double2>(double2 v) { return v; }
-template <> __device__ __forceinline__ float2 cell_out<float2>(double2 v) {
-    return make_float2((float)v.x, (float)v.y);
-}
 
 // Real-space value of each quadrant cell for block entries [t0, t0+tc),
 // written with the parity mirroring into buf[2nx][2ny][tc] (or only the
@@ -827,7 +822,7 @@ __global__ void k_kernels_vtp(const double *__restrict__ lam, int nl, const doub
     const int m = (int)(idx - (long)tr * nl);
     const Trans T0 = trans[tr];
     const int L = a.L;
-    const double2 *Eta = lay, *Ex = lay + (long)L * nl, *P1 = lay + 2L * L * nl, *Q1 = lay + 3L * L * nl;
+    const double2 *Eta = lay, *P1 = lay + 2L * L * nl, *Q1 = lay + 3L * L * nl;
     const double2 *Ps = lay + 4L * L * nl, *Qs = lay + 5L * L * nl;
     const int r = T0.r, s = T0.s, t = min(r, s), b = max(r, s);
     const double l = lam[m];
