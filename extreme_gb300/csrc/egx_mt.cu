@@ -143,10 +143,10 @@ __global__ void k_js(const double2 *__restrict__ zeta, const double2 *__restrict
 }
 
 // Es and jQ (ForwardSolver.CalculateScatteredFieldFromChi / CalculateJqFromScatteredField,
-// ForwardSolver.cs:391-436).
-__global__ void k_post(const double2 *__restrict__ zeta, const double2 *__restrict__ zeta0,
-                       const double2 *__restrict__ chi, const double2 *__restrict__ js, int nz, long ncell,
-                       double2 *__restrict__ jq) {
+// ForwardSolver.cs:391-436). In place: chi and jq may be the same vector
+// (each thread reads its element before writing it).
+__global__ void k_post(const double2 *__restrict__ zeta, const double2 *__restrict__ zeta0, const double2 *chi,
+                       const double2 *__restrict__ js, int nz, long ncell, double2 *jq) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= ncell * 3 * nz) return;
     int k = (int)(idx % nz);
