@@ -1,5 +1,6 @@
 // Device vector kernels and the host-side GMRES driver (see egx_krylov.cuh).
 #include <cmath>
+#include <cstdint>
 
 #include "egx_krylov.cuh"
 
@@ -293,6 +294,9 @@ __global__ void k_f2d_add(const float2 *__restrict__ x, double2 *__restrict__ y,
     }
 }
 
+// the float4 kernels read two complex64 entries per load: 16-byte alignment
+static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
 static int grid_for(long n) {
     long g = (n + kThreads - 1) / kThreads;
     if (g > 2048) g = 2048;
@@ -303,7 +307,7 @@ static int grid_for(long n) {
 template <typename T>
 void VecOps<T>::multi_dot(const C<T> *V, int ncols, const C<T> *w, long n, double2 *dots_dev, double2 *partials,
                           int nblocks, cudaStream_t s) {
-    if (sizeof(T) == sizeof(float) && n % 2 == 0)
+    if (sizeof(T) == sizeof(float) && n % 2 == 0 && aligned16(V) && aligned16(w))
         k_multi_dot_c2<<<nblocks, kThreads, 0, s>>>(reinterpret_cast<const float4 *>(V), ncols,
                                                     reinterpret_cast<const float4 *>(w), n / 2, partials);
     else
@@ -313,7 +317,7 @@ void VecOps<T>::multi_dot(const C<T> *V, int ncols, const C<T> *w, long n, doubl
 template <typename T>
 void VecOps<T>::update_norm(const C<T> *V, int ncols, const double2 *dots_dev, C<T> *w, long n, double *norm2_dev,
                             double *partials, int nblocks, cudaStream_t s) {
-    if (sizeof(T) == sizeof(float) && n % 2 == 0)
+    if (sizeof(T) == sizeof(float) && n % 2 == 0 && aligned16(V) && aligned16(w))
         k_update_norm_c2<<<nblocks, kThreads, 0, s>>>(reinterpret_cast<const float4 *>(V), ncols, dots_dev,
                                                       reinterpret_cast<float4 *>(w), n / 2, partials);
     else
