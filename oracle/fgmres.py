@@ -1,4 +1,4 @@
-"""Oracle: restarted GMRES / flexible GMRES with a GMRES preconditioner,
+"""Oracle (TEST INFRASTRUCTURE ONLY, see ``oracle/__init__.py``): restarted GMRES / flexible GMRES with a GMRES preconditioner,
 numpy complex128, following ``Extreme.Fgmres`` step by step.
 
 * ``GmresSolver.Solve`` (``Extreme.Fgmres/Gmres.cs:77-143``): zero-rhs

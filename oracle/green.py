@@ -1,4 +1,4 @@
-"""Oracle: anomaly-to-anomaly (AtoA) Green tensor of the layered background,
+"""Oracle (TEST INFRASTRUCTURE ONLY, see ``oracle/__init__.py``): anomaly-to-anomaly (AtoA) Green tensor of the layered background,
 restated in numpy complex128 from the reference.
 
 Pipeline (``Extreme.Cartesian/Forward/AtoA/AtoAGreenTensorCalculatorComponent.cs:82-279``):

@@ -1,4 +1,4 @@
-"""Oracle: the MT source field and the CIE pipeline around the solve.
+"""Oracle (TEST INFRASTRUCTURE ONLY, see ``oracle/__init__.py``): the MT source field and the CIE pipeline around the solve.
 
 * 1-D plane-wave field at lambda = 0 (``Extreme.Cartesian.Magnetotellurics/PlaneWaveCalculator.cs:11-83``
   with the single-lambda recursions of ``Green/Scalar/Impl/PlanCalculator.cs:173-314``);

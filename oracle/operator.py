@@ -1,4 +1,4 @@
-"""Oracle: the CIE convolution operator, numpy complex128.
+"""Oracle (TEST INFRASTRUCTURE ONLY, see ``oracle/__init__.py``): the CIE convolution operator, numpy complex128.
 
 Restates ``Extreme.Cartesian/Forward/AtoA/ConvolutionOperator.cs``:
 
