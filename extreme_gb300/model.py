@@ -23,7 +23,7 @@ Depths and thicknesses are C# ``decimal`` in the reference. Here they are
 doubles built from whole centimetres so that sums and comparisons are exact.
 """
 from dataclasses import dataclass, field
-from typing import List, Optional
+from typing import List
 
 import numpy as np
 
