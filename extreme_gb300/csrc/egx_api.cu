@@ -446,6 +446,8 @@ extern "C" {
 
 int egx_version(void) { return 1; }
 
+long egx_device_allocations(void) { return egx::device_allocations().load(); }
+
 int egx_create(int device, egx_ctx **out) {
     if (!out) return EGX_ERR_INVALID;
     *out = nullptr;
@@ -878,6 +880,8 @@ int egx_dot_products(egx_ctx *ctx, const double *V, int ncols, const double *w, 
         set_device(ctx);
         const double2 *dV, *dw;
         if (where == EGX_DEVICE) {
+            EGX_CHECK(aligned16(V) && aligned16(w) && aligned16(out), EGX_ERR_INVALID,
+                      "egx_dot_products: device V, w and out must be 16-byte aligned");
             dV = (const double2 *)V;
             dw = (const double2 *)w;
         } else {

@@ -2,6 +2,7 @@
 // double2/float2, error handling, the context object.
 #pragma once
 
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -142,7 +143,28 @@ struct Timers {
     }
 };
 
-// Device buffer owned by the context.
+// Count of device allocations (cudaMalloc calls that succeeded) the library
+// has made in this process; egx_device_allocations reports it.
+inline std::atomic<long> &device_allocations() {
+    static std::atomic<long> n{0};
+    return n;
+}
+
+// cudaMalloc that counts the allocation; throws EGX_ERR_OOM (with `what`)
+// when it fails.
+inline void *device_alloc(size_t bytes, const char *what) {
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess)
+        throw Error(EGX_ERR_OOM, std::string(what) + ": cudaMalloc of " + std::to_string(bytes) +
+                                     " bytes failed: " + cudaGetErrorString(e));
+    device_allocations()++;
+    return p;
+}
+
+// True when p is 16-byte aligned (float4 / double2 loads).
+inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
 // Raise a kernel's dynamic shared-memory limit to at least `bytes` on the
 // current device; never lower it. The limit belongs to the kernel, not to a
 // context: contexts on other host threads may launch the same kernel with a
@@ -161,6 +183,7 @@ inline void raise_smem_limit(const void *fn, size_t bytes) {
     cur = bytes;
 }
 
+// Device buffer owned by the context.
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
@@ -176,11 +199,7 @@ struct DevBuf {
     void ensure(size_t n) {
         if (n <= bytes) return;
         release();
-        cudaError_t e = cudaMalloc(&p, n);
-        if (e != cudaSuccess) {
-            p = nullptr;
-            throw Error(EGX_ERR_OOM, "cudaMalloc of " + std::to_string(n) + " bytes failed: " + cudaGetErrorString(e));
-        }
+        p = device_alloc(n, "device buffer");
         bytes = n;
     }
     template <typename X> X *as() const { return reinterpret_cast<X *>(p); }

@@ -295,7 +295,6 @@ __global__ void k_f2d_add(const float2 *__restrict__ x, double2 *__restrict__ y,
 }
 
 // the float4 kernels read two complex64 entries per load: 16-byte alignment
-static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
 static int grid_for(long n) {
     long g = (n + kThreads - 1) / kThreads;
@@ -376,10 +375,7 @@ Gmres<T>::Gmres(long n, int m, double tol, int max_restarts, bool check_true, cu
     EGX_CHECK(m >= 1 && m <= 60, EGX_ERR_INVALID, "GMRES buffer length must be in [1, 60]");
     nblocks_ = grid_for(n);
     if (nblocks_ > 1024) nblocks_ = 1024;
-    auto alloc = [](void **p, size_t b) {
-        cudaError_t e = cudaMalloc(p, b);
-        if (e != cudaSuccess) throw Error(EGX_ERR_OOM, std::string("GMRES workspace: ") + cudaGetErrorString(e));
-    };
+    auto alloc = [](void **p, size_t b) { *p = device_alloc(b, "GMRES workspace"); };
     alloc((void **)&V_, sizeof(C<T>) * n * m);
     alloc((void **)&w_, sizeof(C<T>) * n);
     alloc((void **)&r0_, sizeof(C<T>) * n);
@@ -536,8 +532,7 @@ GmresResult Gmres<T>::solve(const C<T> *rhs, const C<T> *x0, C<T> *result) {
     GmresResult res;
     iterations_done_ = 0;
     if (precond && !Z_) {
-        cudaError_t e = cudaMalloc((void **)&Z_, sizeof(C<T>) * n_ * m_);
-        if (e != cudaSuccess) throw Error(EGX_ERR_OOM, "FGMRES preconditioned basis allocation failed");
+        Z_ = static_cast<C<T> *>(device_alloc(sizeof(C<T>) * n_ * m_, "FGMRES preconditioned basis"));
     }
     double bn = norm(rhs);
     bn_ = bn;

@@ -17,8 +17,18 @@
 // Host code may not use the array's name as a device address (on the host it
 // is only a stand-in symbol): the address is looked up with
 // cudaGetSymbolAddress once per device, with that device current, by the
-// first call on that device. Make that first call before any stream capture
-// begins.
+// first call on that device.
+//
+// Every call ends by synchronising the context's stream, so it must not be
+// made while that stream is being captured into a CUDA graph, nor from a
+// CUDA host callback (cudaLaunchHostFunc), where CUDA calls are not allowed.
+// "Inside a solver callback" means an ordinary host function that the
+// solver calls between its own launches, such as the preconditioner or
+// dot-product callback of a host-driven Krylov loop.
+//
+// V, w and out are read and written as double2 (16-byte loads and stores),
+// so each must be 16-byte aligned; a misaligned pointer is rejected with
+// EGX_ERR_INVALID before anything is launched.
 #include <algorithm>
 #include <mutex>
 #include <string>
@@ -122,6 +132,8 @@ extern "C" int egx_dot_products_static(egx_ctx *ctx, const double *V, int ncols,
     if (!ctx) return EGX_ERR_INVALID;
     try {
         EGX_CHECK(V && w && out && n >= 1 && ncols >= 1, EGX_ERR_INVALID, "bad dot-product arguments");
+        EGX_CHECK(aligned16(V) && aligned16(w) && aligned16(out), EGX_ERR_INVALID,
+                  "egx_dot_products_static: V, w and out must be 16-byte aligned device pointers");
         if (ncols > kNaMaxCols)
             throw Error(EGX_ERR_INVALID, "egx_dot_products_static: ncols = " + std::to_string(ncols) +
                                              " exceeds the static scratch limit of " + std::to_string(kNaMaxCols) +

@@ -35,7 +35,9 @@ def load(ref_root, ndec="40"):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # the reference checkout: argument, else EGX_REFERENCE, else "reference" beside this checkout
+    beside = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(HERE))), "reference")
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("EGX_REFERENCE", beside)
     h0, h1 = load(ref_root)
     assert h0.size == 431 and h1.size == 431
     np.savez(os.path.join(HERE, "hankel_ndec40.npz"), h0=h0, h1=h1,

@@ -1,7 +1,7 @@
 """ctypes binding of ``libegx.so`` (the C ABI declared in ``include/egx.h``).
 
 This is the Python face of the drop-in boundary: the same entry points a C#
-P/Invoke layer binds (see INTEGRATION.md). The library must be built
+P/Invoke layer binds. The library must be built
 (``python -m extreme_gb300._build``); there is no fallback when it is missing.
 """
 import ctypes as C
@@ -21,7 +21,8 @@ PRECOND_GMRES, PRECOND_CALLBACK, PRECOND_NONE, PRECOND_LEARNED = 0, 1, 2, 3
 
 # Every symbol the header declares (checked by the ABI test).
 EXPORTS = [
-    "egx_create", "egx_destroy", "egx_last_error", "egx_version", "egx_set_stream", "egx_launch_count",
+    "egx_create", "egx_destroy", "egx_last_error", "egx_version", "egx_device_allocations", "egx_set_stream",
+    "egx_launch_count",
     "egx_green_build", "egx_green_upload", "egx_green_download", "egx_green_free",
     "egx_op_prepare", "egx_op_apply", "egx_op_apply_ds", "egx_op_apply_c64", "egx_fft2d",
     "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products", "egx_dot_products_static",
@@ -98,6 +99,8 @@ def load(path=None):
     lib.egx_set_stream.argtypes = [vp, vp]
     lib.egx_launch_count.argtypes = [vp]
     lib.egx_launch_count.restype = C.c_long
+    lib.egx_device_allocations.argtypes = []
+    lib.egx_device_allocations.restype = C.c_long
     lib.egx_green_build.argtypes = [vp, C.POINTER(Model), d, i, i, C.POINTER(vp)]
     lib.egx_green_upload.argtypes = [vp, i, i, i, C.POINTER(vp), i, C.POINTER(vp)]
     lib.egx_green_download.argtypes = [vp, vp, C.POINTER(vp)]
@@ -183,6 +186,11 @@ class Context:
 
     def launch_count(self):
         return int(self.lib.egx_launch_count(self.h))
+
+    @staticmethod
+    def device_allocations():
+        """Device allocations (cudaMalloc calls) the library has made in this process."""
+        return int(load().egx_device_allocations())
 
     def set_stream(self, stream_handle):
         self._check(self.lib.egx_set_stream(self.h, C.c_void_p(stream_handle)))

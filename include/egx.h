@@ -114,6 +114,10 @@ int egx_create(int device, egx_ctx **out);
 int egx_destroy(egx_ctx *ctx);
 int egx_last_error(egx_ctx *ctx, char *buf, size_t len);
 int egx_version(void);
+/* Device allocations (cudaMalloc calls) this library has made in the
+ * process so far; a diagnostic for callers that must know whether a call
+ * allocates. No counterpart in the reference. */
+long egx_device_allocations(void);
 /* Use an external CUDA stream (cudaStream_t) for all work of this context. */
 int egx_set_stream(egx_ctx *ctx, void *stream);
 /* Count of this library's kernel launches since the context was created. */
@@ -219,18 +223,22 @@ int egx_learned_stats(egx_ctx *ctx, long *uses, long *fallbacks);
 int egx_wait_selftest(egx_ctx *ctx, double limit_ms);
 
 /* DotProductRequest (AnomalyCurrentFgmresSolver.cs:115-130): out[k] =
- * conj(V[:, k])^T w for k < ncols, V column-major with leading dimension n. */
+ * conj(V[:, k])^T w for k < ncols, V column-major with leading dimension n.
+ * With EGX_DEVICE, V, w and out must be 16-byte aligned. */
 int egx_dot_products(egx_ctx *ctx, const double *V, int ncols, const double *w, long n, double *out, int where);
 
 /* egx_dot_products on device pointers (V, w, out in device memory) that
  * allocates nothing -- for callers that cannot allocate device memory where
  * they call it, such as a host whose device memory belongs to its own pool
- * allocator or code inside a solver callback. No counterpart in the
- * reference. The partial sums live in one static device array of 128 KiB
- * that every call on a device shares: at most 64 columns per call (more is
- * EGX_ERR_INVALID, see egx_last_error); calls that overlap on the GPU race.
- * The first call on a device looks the array up (cudaGetSymbolAddress) and
- * should come before any stream capture. */
+ * allocator, or a host function that a host-driven Krylov loop calls between
+ * its launches. No counterpart in the reference. The partial sums live in
+ * one static device array of 128 KiB that every call on a device shares: at
+ * most 64 columns per call (more is EGX_ERR_INVALID, see egx_last_error);
+ * calls that overlap on the GPU race. V, w and out must be 16-byte aligned
+ * (else EGX_ERR_INVALID, nothing launched). The first call on a device looks
+ * the array up (cudaGetSymbolAddress). Every call synchronises the context's
+ * stream: it must not be made while that stream is being captured, nor from
+ * a CUDA host callback (cudaLaunchHostFunc). */
 int egx_dot_products_static(egx_ctx *ctx, const double *V, int ncols, const double *w, long n, double *out);
 
 /* ---- MT source and the CIE pipeline around the solve ------------------- */

@@ -257,19 +257,24 @@ def exp_sums(eta, r, s, t, b, dt, db1, r1, r2, s1, s2):
     er, es, et, eb = eta[r], eta[s], eta[t], eta[b]
 
     def e(z):
-        # sums that the case at hand does not use overflow, as in the reference
-        with np.errstate(over="ignore", invalid="ignore"):
-            return np.exp(z)
-    T = (e(_lin((-r1, er), (-s1, es), (2 * dt, et))) - e(_lin((-r1, er), (-s2, es), (2 * dt, et)))
-         - e(_lin((-r2, er), (-s1, es), (2 * dt, et))) + e(_lin((-r2, er), (-s2, es), (2 * dt, et))))
-    R = (e(_lin((-2 * db1, eb), (s2, es), (r2, er))) - e(_lin((-2 * db1, eb), (s1, es), (r2, er)))
-         - e(_lin((-2 * db1, eb), (s2, es), (r1, er))) + e(_lin((-2 * db1, eb), (s1, es), (r1, er))))
-    ctop = (e(_lin((-s1, es), (r2, er))) - e(_lin((-s2, es), (r2, er)))
-            - e(_lin((-s1, es), (r1, er))) + e(_lin((-s2, es), (r1, er))))
-    cbot = (e(_lin((-r1, er), (s2, es))) - e(_lin((-r1, er), (s1, es)))
-            - e(_lin((-r2, er), (s2, es))) + e(_lin((-r2, er), (s1, es))))
-    first = _lin((-2 * db1, eb), (2 * dt, et))
+        return np.exp(z)
+
+    # The six sums are formed for every (transceiver, lambda), as the
+    # reference's C does (green_scalar.c:86-386); the ones that the
+    # transceiver's layer case does not use can overflow to inf, and their
+    # four-term differences become inf - inf = NaN. Those entries are never
+    # read (scalars_for_item picks the sums of its case), so overflow and
+    # invalid operations are masked here explicitly, for all six sums.
     with np.errstate(over="ignore", invalid="ignore"):
+        T = (e(_lin((-r1, er), (-s1, es), (2 * dt, et))) - e(_lin((-r1, er), (-s2, es), (2 * dt, et)))
+             - e(_lin((-r2, er), (-s1, es), (2 * dt, et))) + e(_lin((-r2, er), (-s2, es), (2 * dt, et))))
+        R = (e(_lin((-2 * db1, eb), (s2, es), (r2, er))) - e(_lin((-2 * db1, eb), (s1, es), (r2, er)))
+             - e(_lin((-2 * db1, eb), (s2, es), (r1, er))) + e(_lin((-2 * db1, eb), (s1, es), (r1, er))))
+        ctop = (e(_lin((-s1, es), (r2, er))) - e(_lin((-s2, es), (r2, er)))
+                - e(_lin((-s1, es), (r1, er))) + e(_lin((-s2, es), (r1, er))))
+        cbot = (e(_lin((-r1, er), (s2, es))) - e(_lin((-r1, er), (s1, es)))
+                - e(_lin((-r2, er), (s2, es))) + e(_lin((-r2, er), (s1, es))))
+        first = _lin((-2 * db1, eb), (2 * dt, et))
         dtop, dbot = _d_sums(e, first, es, er, s1, s2, r1, r2)
     return T, R, ctop, cbot, dtop, dbot
 

@@ -4,8 +4,7 @@
   Applique text fills rows along y and runs along x in single precision
   (``AnomalyLoaderUtils.cs:70-170``); the reader rejects what the reference
   rejects (wrong version, missing sections, short or long lines).
-* The reference's own COMMEMI3D2 example deck parses (when the reference
-  tree is beside this checkout).
+* The reference's own COMMEMI3D2 example deck (a committed fixture) parses.
 * The exporter writes .NET ``E``/``F2`` numbers and the reference's file
   names and column heads (``PlainTextExporter.cs``), and its values equal the
   response formulas (impedance via ``egx_mt_responses``, host arithmetic).
@@ -20,7 +19,9 @@ from extreme_gb300.export import PlainTextExporter, cs_e, read_table, tipper
 from extreme_gb300.forward import LevelResult, MtSolution
 from extreme_gb300.model import MU0, freq_to_omega, random_model
 
-REFERENCE_DECK = "/root/reference/EndUser/ExtremeMt/Examples/COMMEMI3D2"
+# the reference's COMMEMI3D2 example deck (EndUser/ExtremeMt/Examples/COMMEMI3D2),
+# committed as a fixture by tests/golden/copy_commemi3d2.py
+REFERENCE_DECK = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "commemi3d2")
 
 
 def test_model_round_trip(tmp_path):
@@ -111,7 +112,6 @@ def test_project_round_trip_and_defaults(tmp_path):
     assert q.levels == [] and q.sites == []
 
 
-@pytest.mark.skipif(not os.path.isdir(REFERENCE_DECK), reason="reference tree not present")
 def test_reference_example_deck():
     p = pj.read_project(os.path.join(REFERENCE_DECK, "forward.xproj"))
     m = pj.read_model(p.model_path())
