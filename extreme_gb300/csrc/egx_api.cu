@@ -153,6 +153,13 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
         (*outer)->precond = [ctx, net, nrhs, in](const C<T> *src, C<T> *dst) {
             net_apply(net, reinterpret_cast<const float2 *>(src), reinterpret_cast<float2 *>(dst), nrhs, ctx->stream,
                       &ctx->launches);
+            if (ctx->learned_inject > 0) {
+                // test hook (egx_learned_inject_nonfinite): the host overwrites
+                // the network's first output entry with NaN
+                static const float2 kNonFinite = make_float2(__builtin_nanf(""), __builtin_nanf(""));
+                ctx->learned_inject--;
+                EGX_CUDA(cudaMemcpyAsync(dst, &kNonFinite, sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
+            }
             in->solve(src, dst, dst);
         };
     } else if (precond_kind == EGX_PRECOND_CALLBACK) {
@@ -850,6 +857,14 @@ int egx_mixed_solve(egx_ctx *ctx, const double *b, double *x, const egx_mixed_pa
         return fail(ctx, EGX_ERR_INVALID, e.what());
     }
     return status;
+}
+
+int egx_learned_inject_nonfinite(egx_ctx *ctx, int count) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(count >= 0, EGX_ERR_INVALID, "injection count must be >= 0");
+        ctx->learned_inject = count;
+    });
 }
 
 int egx_learned_stats(egx_ctx *ctx, long *uses, long *fallbacks) {

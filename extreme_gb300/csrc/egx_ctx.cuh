@@ -51,6 +51,7 @@ struct egx_ctx {
     std::unique_ptr<egx::Gmres<float>> outer32l, inner32l;
     std::string key32l;
     long learned_uses = 0, learned_fallbacks = 0;
+    int learned_inject = 0;  // test hook: learned outputs still to be overwritten with NaN
     // preconditioner plug
     int precond_kind = EGX_PRECOND_GMRES;
     egx_precond_fn precond_fn = nullptr;

@@ -547,6 +547,12 @@ GmresResult Gmres<T>::solve(const C<T> *rhs, const C<T> *x0, C<T> *result) {
     VecOps<T>::copy(r0_, w_, n_, s_);
     kernel_launches += 1;
     double beta = norm(w_);
+    if (!std::isfinite(beta)) {
+        res.converged = false;
+        res.arnoldi_be = beta;
+        res.true_be = -1;
+        return res;
+    }
     if (beta == 0) {
         if (x0 != result) VecOps<T>::copy(x0, result, n_, s_);
         res.converged = true;
@@ -565,6 +571,17 @@ GmresResult Gmres<T>::solve(const C<T> *rhs, const C<T> *x0, C<T> *result) {
         for (int i = 1; i <= m_; i++) h(i, m_) = 0.0;
         int jh = 0;
         bea = arnoldi(bn, jh);
+        if (!std::isfinite(bea)) {
+            // a non-finite vector (NaN or Inf from the operator or the
+            // preconditioner) never converges: stop at once, not converged,
+            // instead of running out the restarts on NaN (the reference has
+            // no such check; finite runs are unchanged)
+            res.converged = false;
+            res.arnoldi_be = bea;
+            res.true_be = -1;
+            res.iterations = iterations_done_;
+            return res;
+        }
         if (bea < tol_) {
             be = final_actions(jh, rhs, result);
             res.converged = true;

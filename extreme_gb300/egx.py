@@ -30,7 +30,7 @@ EXPORTS = [
     "egx_profile_read",
     "egx_level_fields", "egx_level_cache", "egx_set_level_precision", "egx_mt_responses", "egx_wait_selftest",
     "egx_net_create", "egx_net_free", "egx_net_size", "egx_net_params", "egx_net_set_model", "egx_net_loss_grad",
-    "egx_net_adam", "egx_net_apply", "egx_learned_stats",
+    "egx_net_adam", "egx_net_apply", "egx_learned_stats", "egx_learned_inject_nonfinite",
 ]
 
 # kernel kinds of egx_profile_read
@@ -134,6 +134,7 @@ def load(path=None):
     lib.egx_net_adam.argtypes = [vp, vp, C.c_float]
     lib.egx_net_apply.argtypes = [vp, vp, vp, vp, i, i]
     lib.egx_learned_stats.argtypes = [vp, C.POINTER(C.c_long), C.POINTER(C.c_long)]
+    lib.egx_learned_inject_nonfinite.argtypes = [vp, i]
     lib.egx_profile.argtypes = [vp, i]
     lib.egx_profile_kinds.argtypes = [vp, C.c_uint]
     lib.egx_profile_read.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_double)]
@@ -411,6 +412,11 @@ class Context:
         uses, fb = C.c_long(), C.c_long()
         self._check(self.lib.egx_learned_stats(self.h, C.byref(uses), C.byref(fb)))
         return uses.value, fb.value
+
+    def learned_inject_nonfinite(self, count):
+        """Test hook: the next `count` learned-preconditioner outputs get a
+        NaN written over their first entry from the host."""
+        self._check(self.lib.egx_learned_inject_nonfinite(self.h, int(count)))
 
     def set_precond(self, kind, fn=None):
         """fn(src_ptr, dst_ptr, n, precision) -> None, device pointers."""

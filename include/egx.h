@@ -214,6 +214,13 @@ int egx_net_apply(egx_ctx *ctx, egx_net *net, const float *v, float *z, int batc
  * uses/fallbacks count the inner solves since the context was created.
  * EGX_PRECOND_NONE makes the mixed form's inner FGMRES unpreconditioned. */
 int egx_learned_stats(egx_ctx *ctx, long *uses, long *fallbacks);
+/* Failure-injection hook for tests (no reference counterpart): the next
+ * `count` applications of the learned preconditioner have the first entry of
+ * the network's output overwritten with NaN by a host-to-device copy (no
+ * device-side fault injection), so that the inner solve fails and the
+ * fallback to the GMRES preconditioner runs. A GMRES cycle that meets a
+ * non-finite norm stops at once as not converged. count 0 disarms it. */
+int egx_learned_inject_nonfinite(egx_ctx *ctx, int count);
 
 /* Failure-detection check (no reference counterpart): one kernel waits,
  * through the bounded wait that every TMA-fed kernel uses, on a shared-memory

@@ -126,7 +126,10 @@ class Gmres:
                     break
             H[jh + 1, jh] = dnormw
             if jh < m - 1:
-                V[:, jh + 1] = w / dnormw
+                # at a breakdown (||w|| = 0) the reference divides by zero as
+                # well; that column is NaN and never read (bea is then 0)
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    V[:, jh + 1] = w / dnormw
             for j in range(jh):
                 H[j, jh], H[j + 1, jh] = zrot(H[j, jh], H[j + 1, jh], cs[j], sn[j])
             c, s = zrotg(H[jh, jh], H[jh + 1, jh])

@@ -51,15 +51,19 @@ def prepare(om, op_type):
     return r, fwd, bwd.astype(np.complex128)
 
 
-def contract(G, buf, nz):
+def unpack_blocks(G, nz):
+    """The six components of G as full [.., nz, nz] blocks (xx, xy, yy, zz
+    unpacked from the packed upper storage; xz, yz reshaped)."""
+    return (unpack_symm(G["xx"], nz), unpack_symm(G["xy"], nz), unpack_symm(G["yy"], nz),
+            unpack_symm(G["zz"], nz), G["xz"].reshape(G["xz"].shape[:-1] + (nz, nz)),
+            G["yz"].reshape(G["yz"].shape[:-1] + (nz, nz)))
+
+
+def contract(G, buf, nz, blocks=None):
     """``ApplyGreenTensorAlongZ`` (``ConvolutionOperator.cs:274-327``) on
-    buf[..., 3, nz]; G in the reference layout c -> [.., block]."""
-    sxx = unpack_symm(G["xx"], nz)
-    sxy = unpack_symm(G["xy"], nz)
-    syy = unpack_symm(G["yy"], nz)
-    szz = unpack_symm(G["zz"], nz)
-    axz = G["xz"].reshape(G["xz"].shape[:-1] + (nz, nz))
-    ayz = G["yz"].reshape(G["yz"].shape[:-1] + (nz, nz))
+    buf[..., 3, nz]; G in the reference layout c -> [.., block] (or its
+    ``unpack_blocks`` in ``blocks``)."""
+    sxx, sxy, syy, szz, axz, ayz = blocks if blocks is not None else unpack_blocks(G, nz)
     x = buf[..., 0, :, None]
     y = buf[..., 1, :, None]
     z = buf[..., 2, :, None]
@@ -72,8 +76,10 @@ def contract(G, buf, nz):
     return out
 
 
-def apply(G, om, x, op_type, prepared=None):
-    """One operator application ``y = K x`` on a flat vector."""
+def apply(G, om, x, op_type, prepared=None, blocks=None, chunk=None):
+    """One operator application ``y = K x`` on a flat vector. ``chunk``: the
+    contraction runs over that many rows of the first spectral axis at a
+    time (bounds the unpacked blocks' memory at large sizes; same values)."""
     m = om.model
     nx, ny, nz = m.nx, m.ny, m.nz
     r, fwd, bwd = prepared if prepared is not None else prepare(om, op_type)
@@ -82,7 +88,13 @@ def apply(G, om, x, op_type, prepared=None):
     buf = np.zeros((2 * nx, 2 * ny, 3, nz), np.complex128)
     buf[:nx, :ny] = fwd[None, None, None, :] * rx
     spec = np.fft.fft2(buf, axes=(0, 1))
-    res = contract(G, spec, nz)
+    if chunk is None or blocks is not None:
+        res = contract(G, spec, nz, blocks)
+    else:
+        res = np.empty_like(spec)
+        for i0 in range(0, 2 * nx, chunk):
+            sl = slice(i0, min(2 * nx, i0 + chunk))
+            res[sl] = contract({c: v[sl] for c, v in G.items()}, spec[sl], nz)
     back = np.fft.ifft2(res, axes=(0, 1)) * (4 * nx * ny)
     y = bwd[None, None, None, :] * back[:nx, :ny]
     if op_type == OP_A:
@@ -98,8 +110,9 @@ class Operator:
     def __init__(self, G, om, op_type):
         self.G, self.om, self.op_type = G, om, op_type
         self.prepared = prepare(om, op_type)
+        self.blocks = unpack_blocks(G, om.model.nz)  # unpacked once, the same values every apply
         self.n_applies = 0
 
     def __call__(self, x):
         self.n_applies += 1
-        return apply(self.G, self.om, x, self.op_type, self.prepared)
+        return apply(self.G, self.om, x, self.op_type, self.prepared, self.blocks)
