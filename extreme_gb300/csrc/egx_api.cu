@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <thread>
 
 #include "egx_ctx.cuh"
 #include "egx_learn.cuh"
@@ -613,15 +614,20 @@ int egx_green_download(egx_ctx *ctx, const egx_green *g, double *const comps[6])
         set_device(ctx);
         GreenDims gd{g->nx, g->ny, g->nz};
         const int S = gd.S(), A = gd.A(), Bs = gd.Bs(), lda = gd.lda(), nz = g->nz;
-        std::vector<cd> q((size_t)gd.Q() * Bs);
-        EGX_CUDA(cudaMemcpyAsync(q.data(), g->g64.p, q.size() * sizeof(cd), cudaMemcpyDeviceToHost, ctx->stream));
+        const size_t qn = (size_t)gd.Q() * Bs;
+        std::unique_ptr<cd[]> qbuf(static_cast<cd *>(::operator new[](qn * sizeof(cd))));
+        cd *q = qbuf.get();
+        EGX_CUDA(cudaMemcpyAsync(q, g->g64.p, qn * sizeof(cd), cudaMemcpyDeviceToHost, ctx->stream));
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));
         const int blk[6] = {S, S, S, S, nz * nz, nz * nz};
         const int off[6] = {0, S, 2 * S, 3 * S, 4 * S, 4 * S + A};
         // parity (x, y) of xx, xy, yy, zz, xz, yz
         const int px[6] = {1, -1, 1, 1, -1, 1}, py[6] = {1, -1, 1, 1, 1, -1};
         const int n0 = 2 * g->nx, n1 = 2 * g->ny;
-        for (int kx = 0; kx < n0; kx++)
+        // rows kx split over host threads (the reference layout of a large
+        // tensor is tens of GB)
+        auto rows = [&](int k0, int k1) {
+          for (int kx = k0; kx < k1; kx++)
             for (int ky = 0; ky < n1; ky++) {
                 int a = kx <= g->nx ? kx : n0 - kx;
                 int b = ky <= g->ny ? ky : n1 - ky;
@@ -640,6 +646,16 @@ int egx_green_download(egx_ctx *ctx, const egx_green *g, double *const comps[6])
                     }
                 }
             }
+        };
+        const long work = (long)n0 * n1 * Bs;
+        const int nt = work < (1L << 22) ? 1 : std::max(1, std::min(n0, (int)std::thread::hardware_concurrency()));
+        if (nt == 1) {
+            rows(0, n0);
+        } else {
+            std::vector<std::thread> pool;
+            for (int t = 0; t < nt; t++) pool.emplace_back(rows, (int)((long)n0 * t / nt), (int)((long)n0 * (t + 1) / nt));
+            for (auto &th : pool) th.join();
+        }
     });
 }
 

@@ -36,15 +36,18 @@ def max_threads():
     return int(load().oracle_max_threads())
 
 
-def contract(G, buf, nz, nthreads=0):
+def contract(G, buf, nz, nthreads=0, out=None):
     """Same contract as :func:`oracle.operator.contract`: G maps component ->
     [..., block] complex128 (packed symmetric for xx/xy/yy/zz, [nz*nz] for
-    xz/yz), buf is [..., 3, nz]; returns a new array like buf."""
+    xz/yz), buf is [..., 3, nz]; returns a new array like buf (or fills
+    ``out``, a contiguous complex128 array of buf's shape)."""
     lib = load()
     lead = buf.shape[:-2]
     npts = int(np.prod(lead)) if lead else 1
     comps = [np.ascontiguousarray(G[c], np.complex128) for c in ("xx", "xy", "yy", "zz", "xz", "yz")]
     x = np.ascontiguousarray(buf, np.complex128)
-    out = np.empty_like(x)
+    if out is None:
+        out = np.empty_like(x)
+    assert out.shape == x.shape and out.dtype == np.complex128 and out.flags.c_contiguous
     lib.oracle_contract(npts, nz, *[c.ctypes.data for c in comps], x.ctypes.data, out.ctypes.data, nthreads)
     return out

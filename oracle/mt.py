@@ -134,12 +134,16 @@ class SolveOutput:
     pass
 
 
-def solve_polarization(om, G, pol, m_out=20, m_in=10, tol=1e-8, max_restarts=100):
-    """One source: ``SolveForOneSource`` up to ``jQ``."""
+def solve_polarization(om, G, pol, m_out=20, m_in=10, tol=1e-8, max_restarts=100, make_op=None):
+    """One source: ``SolveForOneSource`` up to ``jQ``. ``make_op(G, om,
+    type)`` builds the prepared operators (default
+    :class:`oracle.operator.Operator`; the CPU baseline passes the threaded
+    one of ``oracle/cpu_apply.py``)."""
+    make_op = make_op or _op.Operator
     e0 = normal_field(om, pol)
     js = scattered_current(om, e0)
-    chi0 = _op.apply(G, om, js, _op.OP_CHI0)
-    A = _op.Operator(G, om, _op.OP_A)
+    chi0 = make_op(G, om, _op.OP_CHI0)(js)
+    A = make_op(G, om, _op.OP_A)
     solver = _fg.fgmres_with_gmres(A, m_out, m_in, tol, max_restarts)
     chi, res = solver.solve(chi0, chi0.copy())
     es = e_scattered(om, chi, js)

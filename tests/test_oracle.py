@@ -215,3 +215,31 @@ def test_fgmres_zero_rhs_shortcut():
     g = fgmres.Gmres(lambda v: 2 * v, 4, 1e-10, 3)
     x, r = g.solve(np.zeros(5, complex), np.ones(5, complex))
     assert r.converged and r.iterations == 0
+
+
+def test_threaded_apply_matches_the_oracle_apply():
+    """The CPU baseline's apply (scipy FFTs on all cores, threaded C
+    contraction) equals the numpy oracle's apply."""
+    from extreme_gb300.model import OmegaModel, scaled_model
+    from oracle import cpu_apply, green
+    from oracle import operator as op
+    m = scaled_model(8, 6, 4, seed=2)
+    om = OmegaModel.build(m, 1.0)
+    G = green.green_tensor(om, 10)
+    x = np.random.default_rng(1).standard_normal(m.nx * m.ny * 3 * m.nz) + 0.5j
+    for t in (op.OP_A, op.OP_CHI0):
+        want = op.apply(G, om, x, t)
+        got = cpu_apply.ThreadedOperator(G, om, t, threads=2)(x)
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-13
+
+
+def test_icgs_pass_orthogonalises():
+    from oracle import cpu_apply
+    rng = np.random.default_rng(4)
+    V, _ = np.linalg.qr(rng.standard_normal((200, 6)) + 1j * rng.standard_normal((200, 6)))
+    w = rng.standard_normal(200) + 1j * rng.standard_normal(200)
+    w0 = w.copy()
+    h, nrm = cpu_apply.icgs_pass(V, 3, w)
+    np.testing.assert_allclose(h, V[:, :4].conj().T @ w0, rtol=1e-13)
+    assert np.abs(V[:, :4].conj().T @ w).max() < 1e-13
+    assert abs(nrm - np.linalg.norm(w)) < 1e-13 * nrm
