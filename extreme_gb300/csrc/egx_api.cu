@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <thread>
 
@@ -91,6 +92,13 @@ void gather_quadrant(int nx, int ny, int nz, const double *const comps[6], std::
         }
 }
 
+// Forget the captured inner-cycle graph (egx_set_graphs).
+void drop_graph(egx_ctx *ctx) {
+    if (ctx->pc_exec) cudaGraphExecDestroy(ctx->pc_exec);
+    ctx->pc_exec = nullptr;
+    ctx->pc_key.clear();
+}
+
 template <typename T>
 GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in, double tol, int max_restarts,
                        bool check_true, int precond_kind, int *n_applies, int nrhs = 1) {
@@ -119,13 +127,24 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
     if (*key != keybuf) {
         if (*outer) ctx->launches += (*outer)->kernel_launches;
         if (*inner) ctx->launches += (*inner)->kernel_launches;
+        drop_graph(ctx);  // a captured inner cycle refers to the old solvers' buffers
         outer->reset();
         inner->reset();
         outer->reset(new Gmres<T>(n, m_out, tol, max_restarts, check_true, ctx->stream));
-        if (precond_kind == EGX_PRECOND_GMRES || precond_kind == EGX_PRECOND_LEARNED)
+        if (precond_kind == EGX_PRECOND_GMRES || precond_kind == EGX_PRECOND_LEARNED) {
             inner->reset(new Gmres<T>(n, m_in, tol, 1, false, ctx->stream));
+            // the inner cycle is enqueued whole: its steps never wait for the host
+            (*inner)->enqueue_only = true;
+        }
         *key = keybuf;
     }
+    // Krylov control on the device (default) or, with EGX_KRYLOV_HOST=1 in
+    // the environment, the host-driven driver that reads every Gram-Schmidt
+    // pass back (the same arithmetic; kept for comparison)
+    const char *host_env = getenv("EGX_KRYLOV_HOST");
+    const bool host_krylov = host_env && host_env[0] == '1';
+    (*outer)->device_control = !host_krylov;
+    if (*inner) (*inner)->device_control = !host_krylov;
     // the inner GMRES runs one cycle to the outer tolerance
     // (FlexibleGmresWithGmresPreconditioner.cs:35-44)
     (*outer)->set_tol(tol);
@@ -135,20 +154,69 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
         apply_dev<T>(ctx, in, out, nrhs);
         applies++;
     };
+    // a device-controlled inner cycle counts its applies on the device (only
+    // those that ran while its cycle was live)
+    auto apply_inner = [ctx, &applies, nrhs, host_krylov](const C<T> *in, C<T> *out) {
+        apply_dev<T>(ctx, in, out, nrhs);
+        if (host_krylov) applies++;
+    };
     (*outer)->apply = apply;
     (*outer)->timers = &ctx->timers;
     if (precond_kind == EGX_PRECOND_GMRES) {
-        (*inner)->apply = apply;
+        (*inner)->apply = apply_inner;
         (*inner)->timers = &ctx->timers;
         Gmres<T> *in = inner->get();
-        (*outer)->precond = [in](const C<T> *src, C<T> *dst) { in->solve(src, src, dst); };
+        if (ctx->use_graphs && !host_krylov && !ctx->timers.on) {
+            // the inner cycle as one CUDA graph: its input and output staged
+            // in fixed buffers, captured once per operator and tolerance
+            // (the graph bakes in every pointer and scalar of the cycle)
+            const size_t vb = (size_t)n * sizeof(C<T>);
+            ctx->pc_in.ensure(vb);
+            ctx->pc_out.ensure(vb);
+            (*outer)->precond = [ctx, in, vb, tol, nrhs](const C<T> *src, C<T> *dst) {
+                C<T> *pin = ctx->pc_in.as<C<T>>(), *pout = ctx->pc_out.as<C<T>>();
+                char key[512];
+                snprintf(key, sizeof key, "%p/%p/%p/%p/%p/%p/%p/%p/%p/%p/%p/%d/%d/%.17g/%zu", (void *)in, ctx->g,
+                         ctx->g->g32.p, ctx->g->g64.p, ctx->r32.p, ctx->r64.p, ctx->buf32.p, ctx->buf64.p,
+                         ctx->tw0_32.p, (void *)pin, (void *)pout, ctx->type, nrhs, tol, vb);
+                EGX_CUDA(cudaMemcpyAsync(pin, src, vb, cudaMemcpyDeviceToDevice, ctx->stream));
+                if (ctx->pc_key != key || !ctx->pc_exec) {
+                    if (ctx->pc_exec) EGX_CUDA(cudaGraphExecDestroy(ctx->pc_exec));
+                    ctx->pc_exec = nullptr;
+                    ctx->pc_key.clear();
+                    cudaGraph_t graph = nullptr;
+                    const long k0 = in->kernel_launches;
+                    EGX_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+                    try {
+                        in->solve(pin, pin, pout);
+                    } catch (...) {
+                        cudaStreamEndCapture(ctx->stream, &graph);
+                        if (graph) cudaGraphDestroy(graph);
+                        throw;
+                    }
+                    EGX_CUDA(cudaStreamEndCapture(ctx->stream, &graph));
+                    const cudaError_t e = cudaGraphInstantiate(&ctx->pc_exec, graph, 0);
+                    cudaGraphDestroy(graph);
+                    EGX_CUDA(e);
+                    ctx->pc_nodes = in->kernel_launches - k0;
+                    in->kernel_launches = k0;
+                    ctx->pc_key = key;
+                }
+                EGX_CUDA(cudaGraphLaunch(ctx->pc_exec, ctx->stream));
+                ctx->launches += ctx->pc_nodes;
+                ctx->pc_replays++;
+                EGX_CUDA(cudaMemcpyAsync(dst, pout, vb, cudaMemcpyDeviceToDevice, ctx->stream));
+            };
+        } else {
+            (*outer)->precond = [in](const C<T> *src, C<T> *dst) { in->solve(src, src, dst); };
+        }
     } else if (precond_kind == EGX_PRECOND_LEARNED) {
         EGX_CHECK(!dbl && ctx->precond_user, EGX_ERR_STATE, "learned preconditioner without a network");
         // the network's estimate of A^-1 v starts the inner GMRES cycle in
         // place of v itself (x0 = v in FlexibleGmresWithGmresPreconditioner.cs:35-44)
         egx_net *net = static_cast<egx_net *>(ctx->precond_user);
         EGX_CHECK(net_length(net) == nvec(ctx), EGX_ERR_INVALID, "learned preconditioner built for another grid");
-        (*inner)->apply = apply;
+        (*inner)->apply = apply_inner;
         (*inner)->timers = &ctx->timers;
         Gmres<T> *in = inner->get();
         (*outer)->precond = [ctx, net, nrhs, in](const C<T> *src, C<T> *dst) {
@@ -176,7 +244,13 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
     } else {
         (*outer)->precond = nullptr;
     }
+    // the inner cycle is enqueued whole: its applies after a stop are
+    // speculative and are not counted (the reference never runs them)
+    Gmres<T> *in = inner->get();
+    const bool spec = in && in->device_control && in->enqueue_only;
+    if (spec) in->reset_apply_counts();
     GmresResult r = (*outer)->solve(b, x, x);
+    if (spec) applies += (int)in->live_applies();
     *n_applies = applies;
     return r;
 }
@@ -274,6 +348,10 @@ void apply_dev(egx_ctx *ctx, const C<T> *x, C<T> *y, int nrhs, bool ds) {
     EGX_CHECK(ctx->g && ctx->type >= 0, EGX_ERR_STATE, "operator is not prepared (PrepareOperator not called)");
     OpDims d{ctx->nx, ctx->ny, ctx->nz, nrhs, nrhs * 3 * ctx->nz, nvec(ctx)};
     d.ds = ds ? 1 : 0;
+    if (sizeof(T) == sizeof(float)) {  // the apply tuner's choices (egx_tune_apply)
+        d.fft_tile = ctx->fft_tile;
+        d.contract_variant = ctx->contract_variant;
+    }
     size_t bufbytes = (size_t)4 * ctx->nx * ctx->ny * d.B * sizeof(C<T>);
     const bool dbl = sizeof(T) == sizeof(double);
     DevBuf &buf = dbl ? ctx->buf64 : ctx->buf32;
@@ -480,10 +558,13 @@ int egx_destroy(egx_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     ctx->timers.flush();
+    drop_graph(ctx);
     ctx->outer64.reset();
     ctx->inner64.reset();
     ctx->outer32.reset();
     ctx->inner32.reset();
+    ctx->outer32l.reset();
+    ctx->inner32l.reset();
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return EGX_OK;
@@ -505,13 +586,98 @@ int egx_set_stream(egx_ctx *ctx, void *stream) {
         if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
         ctx->stream = (cudaStream_t)stream;
         ctx->own_stream = false;
+        // the solvers keep the stream they were made with
+        drop_graph(ctx);
         ctx->outer64.reset();
         ctx->inner64.reset();
         ctx->outer32.reset();
         ctx->inner32.reset();
+        ctx->outer32l.reset();
+        ctx->inner32l.reset();
         ctx->key64.clear();
         ctx->key32.clear();
+        ctx->key32l.clear();
     });
+}
+
+int egx_set_graphs(egx_ctx *ctx, int enable) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        set_device(ctx);
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        drop_graph(ctx);
+        ctx->use_graphs = enable ? 1 : 0;
+    });
+}
+
+int egx_tune_apply(egx_ctx *ctx, int nrhs, int reps, double *ms_out) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(nrhs >= 1 && nrhs <= 16 && reps >= 1 && reps <= 100, EGX_ERR_INVALID, "bad tuning arguments");
+        EGX_CHECK(ctx->g && ctx->type >= 0 && ctx->prepared32, EGX_ERR_STATE,
+                  "tuning needs an operator prepared with a complex64 Green tensor");
+        set_device(ctx);
+        const long n = nvec(ctx) * nrhs;
+        DevBuf xb, yb;
+        xb.ensure(n * sizeof(float2));
+        yb.ensure(n * sizeof(float2));
+        EGX_CUDA(cudaMemsetAsync(xb.p, 0, n * sizeof(float2), ctx->stream));
+        const bool was_on = ctx->timers.on;
+        ctx->timers.on = false;
+        cudaEvent_t a, b;
+        EGX_CUDA(cudaEventCreate(&a));
+        EGX_CUDA(cudaEventCreate(&b));
+        double best = 1e300;
+        int bt = 0, bv = 0;
+        // the packed layout has three contraction kernels to choose from; the
+        // sub-block layout (nz in 16, 32, 48) one
+        const int nvar = sb_layout(ctx->nz) ? 1 : 3;
+        for (int tile = 0; tile < 3; tile++)
+            for (int var = 0; var < nvar; var++) {
+                ctx->fft_tile = tile;
+                ctx->contract_variant = var;
+                apply_dev<float>(ctx, xb.as<float2>(), yb.as<float2>(), nrhs);  // untimed first run
+                EGX_CUDA(cudaEventRecord(a, ctx->stream));
+                for (int r = 0; r < reps; r++) apply_dev<float>(ctx, xb.as<float2>(), yb.as<float2>(), nrhs);
+                EGX_CUDA(cudaEventRecord(b, ctx->stream));
+                EGX_CUDA(cudaEventSynchronize(b));
+                float ms = 0;
+                EGX_CUDA(cudaEventElapsedTime(&ms, a, b));
+                const double per = ms / reps;
+                if (ms_out) ms_out[tile * 3 + var] = per;
+                if (per < best) {
+                    best = per;
+                    bt = tile;
+                    bv = var;
+                }
+            }
+        if (ms_out)
+            for (int var = nvar; var < 3; var++)
+                for (int tile = 0; tile < 3; tile++) ms_out[tile * 3 + var] = -1;
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        ctx->fft_tile = bt;
+        ctx->contract_variant = bv;
+        ctx->timers.on = was_on;
+        check_device_error(ctx);
+    });
+}
+
+int egx_apply_variant(egx_ctx *ctx, int fft_tile, int contract_variant) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(fft_tile >= 0 && fft_tile <= 2 && contract_variant >= 0 && contract_variant <= 2, EGX_ERR_INVALID,
+                  "fft_tile and contract_variant must be in 0..2");
+        ctx->fft_tile = fft_tile;
+        ctx->contract_variant = contract_variant;
+    });
+}
+
+int egx_graph_stats(egx_ctx *ctx, long *replays, long *nodes) {
+    if (!ctx) return EGX_ERR_INVALID;
+    if (replays) *replays = ctx->pc_replays;
+    if (nodes) *nodes = ctx->pc_nodes;
+    return EGX_OK;
 }
 
 long egx_launch_count(egx_ctx *ctx) {

@@ -57,6 +57,15 @@ struct egx_ctx {
     egx_precond_fn precond_fn = nullptr;
     void *precond_user = nullptr;
     egx::DevBuf fftbuf;
+    // egx_set_graphs: the inner GMRES cycle of the flexible preconditioner
+    // captured as one CUDA graph (staging buffers, the executable graph and
+    // the key of everything it bakes in)
+    int use_graphs = 0;
+    int fft_tile = 0, contract_variant = 0;  // egx_tune_apply / egx_apply_variant
+    egx::DevBuf pc_in, pc_out;
+    cudaGraphExec_t pc_exec = nullptr;
+    std::string pc_key;
+    long pc_nodes = 0, pc_replays = 0;
     egx::DevBuf nrm_part, nrm_out, mix_r, mix_t, mix_r32, mix_d32;
     egx::DevBuf js, chi0;
     egx::DevBuf errflag;  // device int: EGX_ERR_TIMEOUT from a bounded wait

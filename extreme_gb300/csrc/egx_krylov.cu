@@ -62,7 +62,8 @@ template <typename T> struct DotRows { static constexpr int value = 8; };
 template <> struct DotRows<double> { static constexpr int value = 4; };
 template <typename T>
 __global__ void k_multi_dot(const C<T> *__restrict__ V, int ncols, const C<T> *__restrict__ w, long n,
-                            double2 *__restrict__ partials) {
+                            double2 *__restrict__ partials, const int *live) {
+    if (live && !*live) return;
     constexpr int ROWS = DotRows<T>::value;
     const long stride = (long)gridDim.x * blockDim.x;
     for (int k0 = 0; k0 < ncols; k0 += kDotCols) {
@@ -106,7 +107,8 @@ __global__ void k_multi_dot(const C<T> *__restrict__ V, int ncols, const C<T> *_
 // (two complex entries), four per column and pass, eight columns per pass
 // (66 registers: three CTAs per SM where sixteen columns allowed two)
 __global__ void k_multi_dot_c2(const float4 *__restrict__ V, int ncols, const float4 *__restrict__ w, long n2,
-                               double2 *__restrict__ partials) {
+                               double2 *__restrict__ partials, const int *live) {
+    if (live && !*live) return;
     constexpr int ROWS = 4, kDotCols = 8;
     const long stride = (long)gridDim.x * blockDim.x;
     auto fma_conj2 = [](float2 &acc, float4 a, float4 b) {  // += conj(a) b, two entries
@@ -156,7 +158,9 @@ __global__ void k_multi_dot_c2(const float4 *__restrict__ V, int ncols, const fl
     }
 }
 
-__global__ void k_reduce_cols(const double2 *__restrict__ partials, int nblocks, int ncols, double2 *__restrict__ out) {
+__global__ void k_reduce_cols(const double2 *__restrict__ partials, int nblocks, int ncols, double2 *__restrict__ out,
+                              const int *live) {
+    if (live && !*live) return;
     const int k = blockIdx.x;
     double2 s = make_double2(0, 0);
     for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
@@ -168,7 +172,9 @@ __global__ void k_reduce_cols(const double2 *__restrict__ partials, int nblocks,
     if (threadIdx.x == 0) out[k] = s;
 }
 
-__global__ void k_reduce_scalar(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
+__global__ void k_reduce_scalar(const double *__restrict__ partials, int nblocks, double *__restrict__ out,
+                                const int *live) {
+    if (live && !*live) return;
     double s = 0;
     for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[b];
     s = block_sum(s);
@@ -177,7 +183,8 @@ __global__ void k_reduce_scalar(const double *__restrict__ partials, int nblocks
 
 template <typename T>
 __global__ void k_update_norm(const C<T> *__restrict__ V, int ncols, const double2 *__restrict__ dots, C<T> *w, long n,
-                              double *__restrict__ partials) {
+                              double *__restrict__ partials, const int *live) {
+    if (live && !*live) return;
     __shared__ C<T> sd[64];
     for (int k = threadIdx.x; k < ncols; k += blockDim.x) sd[k] = mk<T>((T)dots[k].x, (T)dots[k].y);
     __syncthreads();
@@ -204,7 +211,8 @@ __global__ void k_update_norm(const C<T> *__restrict__ V, int ncols, const doubl
 
 // complex64 vectors of even length: the update with float4 loads
 __global__ void k_update_norm_c2(const float4 *__restrict__ V, int ncols, const double2 *__restrict__ dots, float4 *w,
-                                 long n2, double *__restrict__ partials) {
+                                 long n2, double *__restrict__ partials, const int *live) {
+    if (live && !*live) return;
     __shared__ float2 sd[64];
     for (int k = threadIdx.x; k < ncols; k += blockDim.x) sd[k] = make_float2((float)dots[k].x, (float)dots[k].y);
     __syncthreads();
@@ -236,7 +244,8 @@ __global__ void k_update_norm_c2(const float4 *__restrict__ V, int ncols, const 
 }
 
 template <typename T>
-__global__ void k_norm2(const C<T> *__restrict__ x, long n, double *__restrict__ partials) {
+__global__ void k_norm2(const C<T> *__restrict__ x, long n, double *__restrict__ partials, const int *live) {
+    if (live && !*live) return;
     const long stride = (long)gridDim.x * blockDim.x;
     T acc = 0;
     for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
@@ -259,18 +268,31 @@ __global__ void k_divide(const C<T> *__restrict__ x, T d, C<T> *__restrict__ y, 
         y[r] = mk<T>(x[r].x / d, x[r].y / d);
 }
 template <typename T>
-__global__ void k_sub(const C<T> *__restrict__ a, const C<T> *__restrict__ b, C<T> *__restrict__ y, long n) {
+__global__ void k_divide_dev(const C<T> *__restrict__ x, const double *__restrict__ d, C<T> *__restrict__ y, long n,
+                             const int *live) {
+    if (live && !*live) return;
+    const T dd = (T)*d;
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+        y[r] = mk<T>(x[r].x / dd, x[r].y / dd);
+}
+template <typename T>
+__global__ void k_sub(const C<T> *__restrict__ a, const C<T> *__restrict__ b, C<T> *__restrict__ y, long n,
+                      const int *live) {
+    if (live && !*live) return;
     for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
         y[r] = csub<T>(a[r], b[r]);
 }
 template <typename T>
-__global__ void k_add(const C<T> *__restrict__ x, C<T> *__restrict__ y, long n) {
+__global__ void k_add(const C<T> *__restrict__ x, C<T> *__restrict__ y, long n, const int *live) {
+    if (live && !*live) return;
     for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
         y[r] = cadd<T>(y[r], x[r]);
 }
 template <typename T>
 __global__ void k_gemv(const C<T> *__restrict__ V, int ncols, const double2 *__restrict__ coef, C<T> *__restrict__ out,
-                       long n) {
+                       long n, const int *ncols_dev) {
+    if (ncols_dev) ncols = *ncols_dev;
+    if (ncols <= 0) return;
     __shared__ C<T> sc[64];
     for (int k = threadIdx.x; k < ncols; k += blockDim.x) sc[k] = mk<T>((T)coef[k].x, (T)coef[k].y);
     __syncthreads();
@@ -305,28 +327,29 @@ static int grid_for(long n) {
 
 template <typename T>
 void VecOps<T>::multi_dot(const C<T> *V, int ncols, const C<T> *w, long n, double2 *dots_dev, double2 *partials,
-                          int nblocks, cudaStream_t s) {
+                          int nblocks, cudaStream_t s, const int *live) {
     if (sizeof(T) == sizeof(float) && n % 2 == 0 && aligned16(V) && aligned16(w))
         k_multi_dot_c2<<<nblocks, kThreads, 0, s>>>(reinterpret_cast<const float4 *>(V), ncols,
-                                                    reinterpret_cast<const float4 *>(w), n / 2, partials);
+                                                    reinterpret_cast<const float4 *>(w), n / 2, partials, live);
     else
-        k_multi_dot<T><<<nblocks, kThreads, 0, s>>>(V, ncols, w, n, partials);
-    k_reduce_cols<<<ncols, kThreads, 0, s>>>(partials, nblocks, ncols, dots_dev);
+        k_multi_dot<T><<<nblocks, kThreads, 0, s>>>(V, ncols, w, n, partials, live);
+    k_reduce_cols<<<ncols, kThreads, 0, s>>>(partials, nblocks, ncols, dots_dev, live);
 }
 template <typename T>
 void VecOps<T>::update_norm(const C<T> *V, int ncols, const double2 *dots_dev, C<T> *w, long n, double *norm2_dev,
-                            double *partials, int nblocks, cudaStream_t s) {
+                            double *partials, int nblocks, cudaStream_t s, const int *live) {
     if (sizeof(T) == sizeof(float) && n % 2 == 0 && aligned16(V) && aligned16(w))
         k_update_norm_c2<<<nblocks, kThreads, 0, s>>>(reinterpret_cast<const float4 *>(V), ncols, dots_dev,
-                                                      reinterpret_cast<float4 *>(w), n / 2, partials);
+                                                      reinterpret_cast<float4 *>(w), n / 2, partials, live);
     else
-        k_update_norm<T><<<nblocks, kThreads, 0, s>>>(V, ncols, dots_dev, w, n, partials);
-    k_reduce_scalar<<<1, kThreads, 0, s>>>(partials, nblocks, norm2_dev);
+        k_update_norm<T><<<nblocks, kThreads, 0, s>>>(V, ncols, dots_dev, w, n, partials, live);
+    k_reduce_scalar<<<1, kThreads, 0, s>>>(partials, nblocks, norm2_dev, live);
 }
 template <typename T>
-void VecOps<T>::norm2(const C<T> *x, long n, double *norm2_dev, double *partials, int nblocks, cudaStream_t s) {
-    k_norm2<T><<<nblocks, kThreads, 0, s>>>(x, n, partials);
-    k_reduce_scalar<<<1, kThreads, 0, s>>>(partials, nblocks, norm2_dev);
+void VecOps<T>::norm2(const C<T> *x, long n, double *norm2_dev, double *partials, int nblocks, cudaStream_t s,
+                      const int *live) {
+    k_norm2<T><<<nblocks, kThreads, 0, s>>>(x, n, partials, live);
+    k_reduce_scalar<<<1, kThreads, 0, s>>>(partials, nblocks, norm2_dev, live);
 }
 template <typename T>
 void VecOps<T>::scale(const C<T> *x, double a, C<T> *y, long n, cudaStream_t s) {
@@ -337,16 +360,21 @@ void VecOps<T>::divide(const C<T> *x, double d, C<T> *y, long n, cudaStream_t s)
     k_divide<T><<<grid_for(n), kThreads, 0, s>>>(x, (T)d, y, n);
 }
 template <typename T>
-void VecOps<T>::sub(const C<T> *a, const C<T> *b, C<T> *y, long n, cudaStream_t s) {
-    k_sub<T><<<grid_for(n), kThreads, 0, s>>>(a, b, y, n);
+void VecOps<T>::divide_dev(const C<T> *x, const double *d, C<T> *y, long n, cudaStream_t s, const int *live) {
+    k_divide_dev<T><<<grid_for(n), kThreads, 0, s>>>(x, d, y, n, live);
 }
 template <typename T>
-void VecOps<T>::add(const C<T> *x, C<T> *y, long n, cudaStream_t s) {
-    k_add<T><<<grid_for(n), kThreads, 0, s>>>(x, y, n);
+void VecOps<T>::sub(const C<T> *a, const C<T> *b, C<T> *y, long n, cudaStream_t s, const int *live) {
+    k_sub<T><<<grid_for(n), kThreads, 0, s>>>(a, b, y, n, live);
 }
 template <typename T>
-void VecOps<T>::gemv(const C<T> *V, int ncols, const double2 *coef, C<T> *out, long n, cudaStream_t s) {
-    k_gemv<T><<<grid_for(n), kThreads, 0, s>>>(V, ncols, coef, out, n);
+void VecOps<T>::add(const C<T> *x, C<T> *y, long n, cudaStream_t s, const int *live) {
+    k_add<T><<<grid_for(n), kThreads, 0, s>>>(x, y, n, live);
+}
+template <typename T>
+void VecOps<T>::gemv(const C<T> *V, int ncols, const double2 *coef, C<T> *out, long n, cudaStream_t s,
+                     const int *ncols_dev) {
+    k_gemv<T><<<grid_for(n), kThreads, 0, s>>>(V, ncols, coef, out, n, ncols_dev);
 }
 template <typename T>
 void VecOps<T>::copy(const C<T> *x, C<T> *y, long n, cudaStream_t s) {
@@ -385,6 +413,13 @@ Gmres<T>::Gmres(long n, int m, double tol, int max_restarts, bool check_true, cu
     alloc((void **)&coef_, sizeof(double2) * 64);
     alloc((void **)&partials_, sizeof(double2) * (size_t)nblocks_ * 64);
     EGX_CUDA(cudaMallocHost((void **)&host_, sizeof(double2) * 64 + sizeof(double) * 2));
+    alloc((void **)&st_, sizeof(GmState));
+    alloc((void **)&napp_dev_, sizeof(long long));
+    EGX_CUDA(cudaMemsetAsync(napp_dev_, 0, sizeof(long long), s));
+    alloc((void **)&Hd_, sizeof(double2) * (m + 1) * (m + 1));
+    alloc((void **)&csd_, sizeof(double) * m);
+    alloc((void **)&snd_, sizeof(double2) * m);
+    EGX_CUDA(cudaMallocHost((void **)&hst_, sizeof(GmState)));
     H_.assign((size_t)(m + 1) * (m + 1), 0.0);
     cs_.assign(m, 0.0);
     sn_.assign(m, 0.0);
@@ -400,6 +435,12 @@ Gmres<T>::~Gmres() {
     cudaFree(dots_);
     cudaFree(coef_);
     cudaFree(partials_);
+    cudaFree(st_);
+    cudaFree(napp_dev_);
+    cudaFree(Hd_);
+    cudaFree(csd_);
+    cudaFree(snd_);
+    cudaFreeHost(hst_);
     cudaFreeHost(host_);
 }
 
@@ -521,7 +562,6 @@ double Gmres<T>::arnoldi(double bn, int &jh) {
         double dnormres = std::abs(h(jh + 1, m));
         bea = dnormres / bn;
         iterations_done_++;
-        if (on_iteration) on_iteration(iterations_done_, bea);
         jh++;
     } while (bea > tol_ && jh < m);
     return bea;
@@ -529,11 +569,14 @@ double Gmres<T>::arnoldi(double bn, int &jh) {
 
 template <typename T>
 GmresResult Gmres<T>::solve(const C<T> *rhs, const C<T> *x0, C<T> *result) {
+    if (precond && !Z_) Z_ = static_cast<C<T> *>(device_alloc(sizeof(C<T>) * n_ * m_, "FGMRES preconditioned basis"));
+    return device_control ? solve_device(rhs, x0, result) : solve_host(rhs, x0, result);
+}
+
+template <typename T>
+GmresResult Gmres<T>::solve_host(const C<T> *rhs, const C<T> *x0, C<T> *result) {
     GmresResult res;
     iterations_done_ = 0;
-    if (precond && !Z_) {
-        Z_ = static_cast<C<T> *>(device_alloc(sizeof(C<T>) * n_ * m_, "FGMRES preconditioned basis"));
-    }
     double bn = norm(rhs);
     bn_ = bn;
     if (bn == 0) {
@@ -606,6 +649,337 @@ GmresResult Gmres<T>::solve(const C<T> *rhs, const C<T> *x0, C<T> *result) {
     res.arnoldi_be = bea;
     res.true_be = be;
     res.iterations = iterations_done_;
+    return res;
+}
+
+// ------------------------------------------------------------ device control
+//
+// One-thread kernels that take the host's decisions of GmresSolver
+// (Extreme.Fgmres/Gmres.cs:77-348) on the device state GmState: the
+// right-hand side and initial residual norms (:80-107), the classical
+// Gram-Schmidt pass bookkeeping and its re-orthogonalisation test
+// (:252-262, :297-313), the Givens rotations and the Arnoldi backward error
+// (:271-292), and the upper-triangular solve of the solution update
+// (:187-196, SimplifiedZtrsv). The arithmetic is the host driver's, in the
+// same order; complex moduli and quotients use hypot and Smith's division.
+
+__device__ __forceinline__ double cabs2(double2 a) { return hypot(a.x, a.y); }
+__device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cconj2(double2 a) { return make_double2(a.x, -a.y); }
+// x, y <- c x + s y, c y - conj(s) x (zrot)
+__device__ __forceinline__ void zrot_dev(double2 &x, double2 &y, double c, double2 s) {
+    const double2 sy = cmul2(s, y), sx = cmul2(cconj2(s), x);
+    const double2 t = make_double2(c * x.x + sy.x, c * x.y + sy.y);
+    y = make_double2(c * y.x - sx.x, c * y.y - sx.y);
+    x = t;
+}
+
+// a fresh solve: ||rhs|| from its squared norm
+__global__ void k_gm_start(GmState *st, const double *norm2) {
+    GmState g;
+    memset(&g, 0, sizeof g);
+    g.bn = sqrt(*norm2);
+    g.flags = !isfinite(g.bn) ? kGmNonFinite : (g.bn == 0 ? kGmZero : 0);
+    g.active = g.flags == 0;
+    g.true_be = -1;
+    *st = g;
+}
+
+// beta = ||r0||: a cycle starts (active) unless beta is 0 (the initial guess
+// is exact: CheckForExactSolution, one iteration) or not finite
+__global__ void k_gm_beta(GmState *st, const double *norm2, int first) {
+    if (st->flags) return;
+    const double beta = sqrt(*norm2);
+    st->beta = beta;
+    if (!isfinite(beta)) {
+        st->flags |= kGmNonFinite;
+        st->active = 0;
+    } else if (beta == 0) {
+        st->flags |= kGmExact;
+        if (first) st->iterations = 1;
+        st->active = 0;
+    } else {
+        st->active = 1;
+    }
+}
+
+// the rhs column of H = beta e1; no steps yet
+__global__ void k_gm_cycle(GmState *st, double2 *H, int m) {
+    if (!st->active) return;
+    for (int i = threadIdx.x; i <= m; i += blockDim.x)
+        H[(size_t)m * (m + 1) + i] = make_double2(i == 0 ? st->beta : 0.0, 0.0);
+    if (threadIdx.x == 0) st->jh = 0;
+}
+
+// one Gram-Schmidt pass of step j (pass 1: while active; later passes:
+// while the previous one asked for another): h(0..j, j) += dots, dloo,
+// ||w|| and the re-orthogonalisation test 2 ||w|| <= sqrt(dloo)
+__global__ void k_gm_ortho(GmState *st, double2 *H, const double2 *dots, const double *norm2, int j, int m,
+                           int pass, int max_pass) {
+    if (!(pass == 1 ? st->active : st->reorth)) return;
+    double2 *h = H + (size_t)j * (m + 1);
+    double ss = 0;
+    for (int i = 0; i <= j; i++) {
+        const double2 d = dots[i];
+        const double2 o = pass == 1 ? make_double2(0.0, 0.0) : h[i];
+        h[i] = make_double2(o.x + d.x, o.y + d.y);
+        ss += d.x * d.x + d.y * d.y;
+    }
+    st->dloo = ss;
+    st->dnormw = sqrt(*norm2);
+    st->reorth = (2.0 * st->dnormw <= sqrt(ss) && pass < max_pass) ? 1 : 0;
+}
+
+// the rest of step j: h(j+1, j) = ||w||, the previous rotations, zrotg,
+// the rotation of the rhs column, bea = |g_{j+1}| / ||b||; the cycle stops
+// when bea <= tol, after m steps, or on a non-finite bea
+__global__ void k_gm_step(GmState *st, double2 *H, double *cs, double2 *sn, int j, int m, double tol) {
+    if (!st->active) return;
+    double2 *h = H + (size_t)j * (m + 1);
+    double2 *g = H + (size_t)m * (m + 1);
+    h[j + 1] = make_double2(st->dnormw, 0.0);
+    for (int i = 0; i < j; i++) zrot_dev(h[i], h[i + 1], cs[i], sn[i]);
+    {  // zrotg (classic reference algorithm)
+        const double2 a = h[j], b = h[j + 1];
+        double c;
+        double2 sv;
+        const double aa = cabs2(a);
+        if (aa == 0.0) {
+            c = 0.0;
+            sv = make_double2(1.0, 0.0);
+        } else {
+            const double scale = aa + cabs2(b);
+            const double a1 = cabs2(make_double2(a.x / scale, a.y / scale));
+            const double b1 = cabs2(make_double2(b.x / scale, b.y / scale));
+            const double nrm = scale * sqrt(a1 * a1 + b1 * b1);
+            const double2 alpha = make_double2(a.x / aa, a.y / aa);
+            c = aa / nrm;
+            const double2 t = cmul2(alpha, cconj2(b));
+            sv = make_double2(t.x / nrm, t.y / nrm);
+        }
+        cs[j] = c;
+        sn[j] = sv;
+    }
+    zrot_dev(g[j], g[j + 1], cs[j], sn[j]);
+    zrot_dev(h[j], h[j + 1], cs[j], sn[j]);
+    h[j + 1] = make_double2(0.0, 0.0);
+    const double bea = cabs2(g[j + 1]) / st->bn;
+    st->bea = bea;
+    st->iterations++;
+    st->jh = j + 1;
+    if (!isfinite(bea)) st->flags |= kGmNonFinite;
+    if (!(bea > tol && j + 1 < m)) st->active = 0;
+}
+
+// y = H(0:jh, 0:jh) \ g (upper triangular, SimplifiedZtrsv) into coef;
+// ncols = jh, or 0 when the solve ended before a cycle (zero rhs, exact
+// guess, non-finite)
+__global__ void k_gm_construct(GmState *st, const double2 *H, int m, double2 *coef) {
+    const int jh = (st->flags & (kGmZero | kGmNonFinite)) || ((st->flags & kGmExact) && st->jh == 0) ? 0 : st->jh;
+    for (int i = 0; i < jh; i++) coef[i] = H[(size_t)m * (m + 1) + i];
+    for (int j = jh - 1; j >= 0; j--) {
+        double2 y = coef[j];
+        if (y.x != 0.0 || y.y != 0.0) {
+            y = cdiv<double>(y, H[(size_t)j * (m + 1) + j]);
+            coef[j] = y;
+            for (int i = j - 1; i >= 0; i--) {
+                const double2 t = cmul2(y, H[(size_t)j * (m + 1) + i]);
+                coef[i] = make_double2(coef[i].x - t.x, coef[i].y - t.y);
+            }
+        }
+    }
+    st->ncols = jh;
+}
+
+// true backward error ||b - A x|| / ||b||
+__global__ void k_gm_true(GmState *st, const double *norm2) {
+    st->true_be = st->flags & kGmZero ? 0.0 : sqrt(*norm2) / st->bn;
+}
+
+__global__ void k_gm_count(const int *live, long long *count) {
+    if (*live) ++*count;
+}
+
+// an operator apply of the solve; in an enqueue-only solve it may be
+// speculative (its cycle already stopped): it runs all the same, but only a
+// live one is counted (on the device)
+template <typename T>
+void Gmres<T>::apply_counted(const C<T> *x, C<T> *y, const int *live) {
+    apply(x, y);
+    if (enqueue_only) {
+        k_gm_count<<<1, 1, 0, s_>>>(live, napp_dev_);
+        kernel_launches += 1;
+    }
+}
+
+template <typename T>
+long Gmres<T>::live_applies() {
+    long long v = 0;
+    EGX_CUDA(cudaMemcpyAsync(&v, napp_dev_, sizeof v, cudaMemcpyDeviceToHost, s_));
+    EGX_CUDA(cudaStreamSynchronize(s_));
+    return (long)v;
+}
+
+template <typename T>
+void Gmres<T>::reset_apply_counts() {
+    EGX_CUDA(cudaMemsetAsync(napp_dev_, 0, sizeof(long long), s_));
+}
+
+template <typename T>
+void Gmres<T>::dc_norm(const C<T> *x, const int *live) {
+    VecOps<T>::norm2(x, n_, norm_dev_, reinterpret_cast<double *>(partials_), nblocks_, s_, live);
+    kernel_launches += 2;
+}
+
+template <typename T>
+GmState Gmres<T>::read_state() {
+    EGX_CUDA(cudaMemcpyAsync(hst_, st_, sizeof(GmState), cudaMemcpyDeviceToHost, s_));
+    EGX_CUDA(cudaStreamSynchronize(s_));
+    return *hst_;
+}
+
+// w = rhs - A x (x: the initial guess or the current solution, never one of
+// this solver's vectors) and beta = ||w||; first: the initial residual
+// (predicated on a non-zero right-hand side)
+template <typename T>
+void Gmres<T>::dc_residual(const C<T> *rhs, const C<T> *x, bool first) {
+    const int *live = first ? &st_->active : nullptr;
+    apply_counted(x, r0_, &st_->active);
+    VecOps<T>::sub(rhs, r0_, w_, n_, s_, live);
+    kernel_launches += 1;
+    dc_norm(w_, live);
+    k_gm_beta<<<1, 1, 0, s_>>>(st_, norm_dev_, first ? 1 : 0);
+    kernel_launches += 1;
+}
+
+// Arnoldi step j of the cycle (KrylovSubspaceConstruction, one iteration)
+template <typename T>
+void Gmres<T>::dc_step(int j) {
+    const int *live = &st_->active;
+    const int *more = &st_->reorth;
+    C<T> *vj = V_ + (long)j * n_;
+    if (precond) {
+        C<T> *zj = Z_ + (long)j * n_;
+        precond(vj, zj);
+        apply_counted(zj, w_, live);
+    } else {
+        apply_counted(vj, w_, live);
+    }
+    const int koff = sizeof(T) == sizeof(double) ? 0 : EGX_K_C64;
+    for (int pass = 1; pass <= 3; pass++) {
+        const int *p = pass == 1 ? live : more;
+        int ev = timers ? timers->begin(EGX_K_GS_DOTS + koff, s_) : -1;
+        VecOps<T>::multi_dot(V_, j + 1, w_, n_, dots_, partials_, nblocks_, s_, p);
+        if (timers) timers->end(ev, s_);
+        ev = timers ? timers->begin(EGX_K_GS_UPDATE + koff, s_) : -1;
+        VecOps<T>::update_norm(V_, j + 1, dots_, w_, n_, norm_dev_, reinterpret_cast<double *>(partials_), nblocks_,
+                               s_, p);
+        if (timers) timers->end(ev, s_);
+        k_gm_ortho<<<1, 1, 0, s_>>>(st_, Hd_, dots_, norm_dev_, j, m_, pass, 3);
+        kernel_launches += 5;
+    }
+    if (j < m_ - 1) {
+        VecOps<T>::divide_dev(w_, &st_->dnormw, V_ + (long)(j + 1) * n_, n_, s_, live);
+        kernel_launches += 1;
+    }
+    k_gm_step<<<1, 1, 0, s_>>>(st_, Hd_, csd_, snd_, j, m_, tol_);
+    kernel_launches += 1;
+}
+
+// ConstructCurrentSolution: result += (Z or V)[:, :jh] y
+template <typename T>
+void Gmres<T>::dc_construct(C<T> *result) {
+    k_gm_construct<<<1, 1, 0, s_>>>(st_, Hd_, m_, coef_);
+    VecOps<T>::gemv(precond ? Z_ : V_, m_, coef_, r0_, n_, s_, &st_->ncols);
+    VecOps<T>::add(r0_, result, n_, s_, &st_->ncols);
+    kernel_launches += 3;
+}
+
+template <typename T>
+GmresResult Gmres<T>::solve_device(const C<T> *rhs, const C<T> *x0, C<T> *result) {
+    GmresResult res;
+    const int *live = &st_->active;
+    dc_norm(rhs, nullptr);
+    k_gm_start<<<1, 1, 0, s_>>>(st_, norm_dev_);
+    kernel_launches += 1;
+    if (!enqueue_only) {  // the reference applies nothing for a zero right-hand side
+        const GmState g = read_state();
+        if (g.flags & kGmZero) {
+            res.converged = true;
+            res.arnoldi_be = res.true_be = 0;
+            return res;
+        }
+        if (g.flags) {
+            res.arnoldi_be = g.bn;
+            return res;
+        }
+    }
+    dc_residual(rhs, x0, true);
+    if (x0 != result) VecOps<T>::copy(x0, result, n_, s_);
+    // one true-residual evaluation at the end (FinalActions / CheckBackwardError)
+    auto true_be = [&]() {
+        if (!check_true_) return -1.0;
+        dc_residual(rhs, result, false);
+        k_gm_true<<<1, 1, 0, s_>>>(st_, norm_dev_);
+        kernel_launches += 1;
+        return read_state().true_be;
+    };
+    int iter = 0;
+    GmState g{};
+    while (true) {
+        if (!enqueue_only) {
+            g = read_state();
+            if (g.flags & kGmExact) {  // CheckForExactSolution, or a zero residual at a restart
+                res.converged = true;
+                res.arnoldi_be = res.true_be = 0;
+                res.iterations = g.iterations;
+                return res;
+            }
+            if (g.flags) {  // non-finite residual
+                res.arnoldi_be = g.beta;
+                res.iterations = g.iterations;
+                return res;
+            }
+        }
+        // V[:, 0] = w / beta, g = beta e1
+        VecOps<T>::divide_dev(w_, &st_->beta, V_, n_, s_, live);
+        k_gm_cycle<<<1, 32, 0, s_>>>(st_, Hd_, m_);
+        kernel_launches += 2;
+        for (int j = 0; j < m_; j++) {
+            dc_step(j);
+            if (!enqueue_only) {
+                g = read_state();
+                if (!g.active) break;
+            }
+        }
+        if (enqueue_only) break;  // one cycle, the device decides everything
+        if (g.flags & kGmNonFinite) {
+            res.arnoldi_be = g.bea;
+            res.iterations = g.iterations;
+            return res;
+        }
+        if (g.bea < tol_) {  // FinalActions
+            dc_construct(result);
+            res.converged = true;
+            res.arnoldi_be = g.bea;
+            res.iterations = g.iterations;
+            res.true_be = true_be();
+            return res;
+        }
+        iter++;
+        if (iter >= max_restarts_) break;
+        // PrepareRestart with the true residual
+        dc_construct(result);
+        dc_residual(rhs, result, false);
+    }
+    // not converged within the restarts (or the enqueue-only single cycle)
+    dc_construct(result);
+    if (enqueue_only) return res;
+    res.arnoldi_be = g.bea;
+    res.iterations = g.iterations;
+    res.true_be = true_be();
     return res;
 }
 

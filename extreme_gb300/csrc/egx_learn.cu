@@ -1,21 +1,23 @@
-// Learned flexible preconditioner: a spectral network that proposes the
-// correction z - v, z ~ A^-1 v, from the residual v and the log-conductivity;
-// the solver starts the inner GMRES cycle of the FGMRES right preconditioner
-// from v + correction (RightPreconditionerRequest plug point,
-// Extreme.Fgmres/FlexibleGmresSolver.cs:24-36). Trained on (residual,
-// A^-1 v - v) pairs, with the forward and backward passes on BF16 tensor-core
-// GEMMs (mma.sync m16n8k16, FP32 accumulation) and Adam, all in this file.
+// Learned flexible preconditioner: a spectral network z = N(v) used as the
+// right preconditioner of the complex64 inner FGMRES of the mixed form (the
+// RightPreconditionerRequest plug point, Extreme.Fgmres/FlexibleGmresSolver.cs:24-36),
+// trained on (residual v, GMRES-preconditioner output) pairs that the solver
+// generates, with the forward and backward passes on BF16 tensor-core GEMMs
+// (mma.sync m16n8k16, FP32 accumulation) and Adam, all in this file.
 //
-// Network, per sample on the nx x ny lateral grid (channels last):
-//   input  X0[x][y][7 nz]: Re and Im of the 3 components of v / rms(v) per
-//          layer (6 nz), log10(omega mu0 sigma dx dy) per layer (nz)
-//   lift   H0 = X0 P + bP                                  (7nz -> width)
-//   L layers  H_{l+1} = act(S_l(H_l) + H_l Wp_l + b_l), act = GELU (tanh
-//          form) on all but the last, S_l = Bx (Wm_l . (Bx^T H By)) By^T:
-//          16 x 16 retained lateral modes in a real Fourier basis (cos 0..7,
-//          sin 1..8 per direction, unit columns), a width x width channel
-//          mixing per mode
-//   output Out = H_L Q + bQ                                (width -> 6 nz)
+// Network, per sample on the nx x ny x nz anomaly mesh (depth is a spatial
+// axis), channels last; on the device sample b is stored as nz slices, row
+// ((b nz + z) nx + x) ny + y of every activation:
+//   input  X0[z][x][y][7]: Re of the 3 components of v / rms(v), Im of the
+//          3 components, log10(omega mu0 sigma dx dy) of the cell
+//   lift   H0 = X0 P + bP                                  (7 -> width)
+//   L layers  H_{l+1} = act(S_l(H_l) + H_l Wp_l + Dz_l H_l + b_l),
+//          act = GELU (tanh form) on all but the last,
+//          S_l = Bx (Wm_l . (Bx^T H[z] By)) By^T per depth slice: 16 x 16
+//          retained lateral modes in a real Fourier basis (cos 0..7, sin 1..8
+//          per direction, unit columns), a width x width channel mixing per
+//          mode shared by all depths; Dz_l: an nz x nz depth mixing per layer
+//   output Out = H_L Q + bQ                                (width -> 6)
 //   z = v + rms(v) (Out_Re + i Out_Im); Q starts at zero, so an untrained
 //   network is the identity preconditioner.
 // Loss per batch: mean over samples of |Out - T|^2 / |T|^2 with T = (z* - v)
@@ -211,55 +213,53 @@ __global__ void k_rms(const double *sum, long n, int batch, float *inv, float *r
     inv[b] = r > 0 ? (float)(1.0 / r) : 0.f;
 }
 
-// X0[b][cell][ch]: Re, Im of the 3 components per layer scaled by inv[b],
-// then the log-conductivity per layer
+// X0[row][ch], row = (b nz + z) ncell + cell: Re of the 3 components, Im of
+// the 3 components (scaled by inv[b]), the log-conductivity of model
+// b % nmodels
 __global__ void k_encode(const float2 *__restrict__ v, const float *__restrict__ inv, const float *__restrict__ logsig,
-                         long ncell, int nz, int batch, float *X) {
-    const int cin = 7 * nz, per = 3 * nz;
-    const long total = (long)batch * ncell * cin;
+                         int nmodels, long ncell, int nz, int batch, float *X) {
+    const long N = ncell * 3 * nz, total = (long)batch * nz * ncell * 7;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % cin);
-        const long rc = i / cin, cell = rc % ncell;
-        const int b = (int)(rc / ncell);
+        const int ch = (int)(i % 7);
+        const long row = i / 7, cell = row % ncell, s = row / ncell;
+        const int z = (int)(s % nz), b = (int)(s / nz);
         float val;
-        if (ch < 2 * per) {
-            const int part = ch / per, e = ch - part * per;  // e = c nz + k
-            const float2 x = v[((long)b * ncell + cell) * per + e];
-            val = (part ? x.y : x.x) * inv[b];
+        if (ch < 6) {
+            const int c = ch % 3;
+            const float2 x = v[(long)b * N + (cell * 3 + c) * nz + z];
+            val = (ch < 3 ? x.x : x.y) * inv[b];
         } else {
-            val = logsig[cell * nz + (ch - 2 * per)];
+            val = logsig[((long)(b % nmodels) * ncell + cell) * nz + z];
         }
         X[i] = val;
     }
 }
 
-// the target in the output layout: (t / rms(v)) as [Re | Im] of 3 nz
+// the target in the output layout T[row][6]: Re | Im of t / rms(v)
 __global__ void k_encode_target(const float2 *__restrict__ t, const float *__restrict__ inv, long ncell, int nz,
                                 int batch, float *T) {
-    const int per = 3 * nz, cout = 6 * nz;
-    const long total = (long)batch * ncell * cout;
+    const long N = ncell * 3 * nz, total = (long)batch * nz * ncell * 6;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % cout);
-        const long rc = i / cout, cell = rc % ncell;
-        const int b = (int)(rc / ncell);
-        const int part = ch / per, e = ch - part * per;
-        const float2 x = t[((long)b * ncell + cell) * per + e];
-        T[i] = (part ? x.y : x.x) * inv[b];
+        const int ch = (int)(i % 6), c = ch % 3;
+        const long row = i / 6, cell = row % ncell, s = row / ncell;
+        const int z = (int)(s % nz), b = (int)(s / nz);
+        const float2 x = t[(long)b * N + (cell * 3 + c) * nz + z];
+        T[i] = (ch < 3 ? x.x : x.y) * inv[b];
     }
 }
 
-// z = v + rms (Out_Re + i Out_Im)
+// z = v + rms (Out_Re + i Out_Im), back in the anomaly layout
 __global__ void k_decode(const float2 *__restrict__ v, const float *__restrict__ rms, const float *__restrict__ out,
                          long ncell, int nz, int batch, float2 *z) {
-    const int per = 3 * nz, cout = 6 * nz;
-    const long total = (long)batch * ncell * per;
+    const long N = ncell * 3 * nz, total = (long)batch * N;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const int e = (int)(i % per);
-        const long rc = i / per;
-        const int b = (int)(rc / ncell);
+        const int b = (int)(i / N);
+        const long e = i - (long)b * N, cell = e / (3 * nz);
+        const int c = (int)((e / nz) % 3), zz = (int)(e % nz);
+        const long row = ((long)b * nz + zz) * ncell + cell;
         const float r = rms[b];
         const float2 x = v[i];
-        z[i] = make_float2(x.x + r * out[rc * cout + e], x.y + r * out[rc * cout + per + e]);
+        z[i] = make_float2(x.x + r * out[row * 6 + c], x.y + r * out[row * 6 + 3 + c]);
     }
 }
 
@@ -317,8 +317,9 @@ unsigned blocks_for(long n) { return (unsigned)std::min<long>((n + 255) / 256, 1
 struct egx_net {
     int nx = 0, ny = 0, nz = 0, W = 0, L = 0, cin = 0, cout = 0;
     long ncell = 0, n_params = 0;
+    int nmodels = 0;  // conductivity models set (sample b uses model b % nmodels)
     long off_P = 0, off_bP = 0, off_Q = 0, off_bQ = 0;
-    std::vector<long> off_Wm, off_Wp, off_b;
+    std::vector<long> off_Wm, off_Wp, off_Dz, off_b;
     egx::DevBuf params, grads, adam_m, adam_v, bx, by, logsig;
     int step = 0, cap = 0;
     // activations of the last forward pass (batch <= cap)
@@ -334,7 +335,8 @@ namespace {
 
 void ensure_batch(egx_net *n, int batch) {
     if (batch <= n->cap) return;
-    const long rows = (long)batch * n->ncell, W = n->W;
+    const long S = (long)batch * n->nz;  // depth slices of the batch
+    const long rows = S * n->ncell, W = n->W;
     n->X0.ensure(rows * n->cin * sizeof(float));
     n->Out.ensure(rows * n->cout * sizeof(float));
     n->T.ensure(rows * n->cout * sizeof(float));
@@ -342,17 +344,17 @@ void ensure_batch(egx_net *n, int batch) {
     for (int l = 0; l <= n->L; l++) n->H[l].ensure(rows * W * sizeof(float));
     for (int l = 0; l < n->L; l++) {
         n->Pre[l].ensure(rows * W * sizeof(float));
-        n->U[l].ensure((size_t)batch * KM * KM * W * sizeof(float));
+        n->U[l].ensure((size_t)S * KM * KM * W * sizeof(float));
     }
-    n->U1.ensure((size_t)batch * KM * n->ny * W * sizeof(float));
-    n->V.ensure((size_t)batch * KM * KM * W * sizeof(float));
-    n->S1.ensure((size_t)batch * n->nx * KM * W * sizeof(float));
+    n->U1.ensure((size_t)S * KM * n->ny * W * sizeof(float));
+    n->V.ensure((size_t)S * KM * KM * W * sizeof(float));
+    n->S1.ensure((size_t)S * n->nx * KM * W * sizeof(float));
     n->dH.ensure(rows * W * sizeof(float));
     n->dH2.ensure(rows * W * sizeof(float));
-    n->dS1.ensure((size_t)batch * n->nx * KM * W * sizeof(float));
-    n->dV.ensure((size_t)batch * KM * KM * W * sizeof(float));
-    n->dU.ensure((size_t)batch * KM * KM * W * sizeof(float));
-    n->dU1.ensure((size_t)batch * KM * n->ny * W * sizeof(float));
+    n->dS1.ensure((size_t)S * n->nx * KM * W * sizeof(float));
+    n->dV.ensure((size_t)S * KM * KM * W * sizeof(float));
+    n->dU.ensure((size_t)S * KM * KM * W * sizeof(float));
+    n->dU1.ensure((size_t)S * KM * n->ny * W * sizeof(float));
     n->sums.ensure(3 * (size_t)batch * sizeof(double));
     n->scal.ensure(2 * (size_t)batch * sizeof(float));
     n->cap = batch;
@@ -375,10 +377,12 @@ GemmArgs wgrad(GemmArgs g) {
     return g;
 }
 
-// X0 (encoded) -> Out; keeps the activations for backward
+// X0 (encoded) -> Out; keeps the activations for backward. The B samples
+// are B nz depth slices for the lateral operations.
 void forward(egx_net *n, int B, cudaStream_t s, long *launches) {
-    const int nx = n->nx, ny = n->ny, W = n->W;
-    const long rows = (long)B * n->ncell;
+    const int nx = n->nx, ny = n->ny, W = n->W, nz = n->nz;
+    const int S = B * nz;
+    const long rows = (long)S * n->ncell, slab = n->ncell * W;
     const float *bx = n->bx.as<float>(), *by = n->by.as<float>();
     gemm(ga((int)rows, W, n->cin, 1, n->X0.as<float>(), n->cin, 1, 0, n->p(n->off_P), W, 1, 0, n->H[0].as<float>(), W,
             1, 0),
@@ -389,24 +393,28 @@ void forward(egx_net *n, int B, cudaStream_t s, long *launches) {
         const float *Hl = n->H[l].as<float>();
         float *U1 = n->U1.as<float>(), *Ul = n->U[l].as<float>(), *V = n->V.as<float>(), *S1 = n->S1.as<float>();
         float *Pre = n->Pre[l].as<float>();
-        // U1[b] = Bx^T H[b]                     (KM x ny W)
-        gemm(ga(KM, ny * W, nx, B, bx, 1, KM, 0, Hl, (long)ny * W, 1, (long)nx * ny * W, U1, (long)ny * W, 1,
+        // U1[s] = Bx^T H[s]                     (KM x ny W) per depth slice s
+        gemm(ga(KM, ny * W, nx, S, bx, 1, KM, 0, Hl, (long)ny * W, 1, (long)nx * ny * W, U1, (long)ny * W, 1,
                 (long)KM * ny * W),
              s, launches);
-        // U[b, i] = By^T U1[b, i]              (KM x W)
-        gemm(ga(KM, W, ny, B * KM, by, 1, KM, 0, U1, W, 1, (long)ny * W, Ul, W, 1, (long)KM * W), s, launches);
-        // V[:, mode] = U[:, mode] Wm[mode]      (B x W) per mode
-        gemm(ga(B, W, W, KM * KM, Ul, (long)KM * KM * W, 1, W, n->p(n->off_Wm[l]), W, 1, (long)W * W, V,
+        // U[s, i] = By^T U1[s, i]              (KM x W)
+        gemm(ga(KM, W, ny, S * KM, by, 1, KM, 0, U1, W, 1, (long)ny * W, Ul, W, 1, (long)KM * W), s, launches);
+        // V[:, mode] = U[:, mode] Wm[mode]      (S x W) per mode
+        gemm(ga(S, W, W, KM * KM, Ul, (long)KM * KM * W, 1, W, n->p(n->off_Wm[l]), W, 1, (long)W * W, V,
                 (long)KM * KM * W, 1, W),
              s, launches);
-        // S1[b] = Bx V[b]                       (nx x KM W)
-        gemm(ga(nx, KM * W, KM, B, bx, KM, 1, 0, V, (long)KM * W, 1, (long)KM * KM * W, S1, (long)KM * W, 1,
+        // S1[s] = Bx V[s]                       (nx x KM W)
+        gemm(ga(nx, KM * W, KM, S, bx, KM, 1, 0, V, (long)KM * W, 1, (long)KM * KM * W, S1, (long)KM * W, 1,
                 (long)nx * KM * W),
              s, launches);
-        // Pre[b, x] = By S1[b, x]               (ny x W)
-        gemm(ga(ny, W, KM, B * nx, by, KM, 1, 0, S1, W, 1, (long)KM * W, Pre, W, 1, (long)ny * W), s, launches);
+        // Pre[s, x] = By S1[s, x]               (ny x W)
+        gemm(ga(ny, W, KM, S * nx, by, KM, 1, 0, S1, W, 1, (long)KM * W, Pre, W, 1, (long)ny * W), s, launches);
         // Pre += H Wp
         gemm(ga((int)rows, W, W, 1, Hl, W, 1, 0, n->p(n->off_Wp[l]), W, 1, 0, Pre, W, 1, 0, 1.f), s, launches);
+        // Pre[b, z] += sum_z' Dz[z, z'] H[b, z']   (nz x ncell W) per sample
+        gemm(ga(nz, (int)slab, nz, B, n->p(n->off_Dz[l]), nz, 1, 0, Hl, slab, 1, (long)nz * slab, Pre, slab, 1,
+                (long)nz * slab, 1.f),
+             s, launches);
         k_bias_act<<<blocks_for(rows * W), 256, 0, s>>>(Pre, n->p(n->off_b[l]), rows, W, l < n->L - 1 ? 1 : 0,
                                                          n->H[l + 1].as<float>());
         if (launches) ++*launches;
@@ -428,8 +436,9 @@ void colsum(const float *x, long rows, int cols, float *out, cudaStream_t s, lon
 
 // dOut -> grads (zeroed here)
 void backward(egx_net *n, int B, cudaStream_t s, long *launches) {
-    const int nx = n->nx, ny = n->ny, W = n->W;
-    const long rows = (long)B * n->ncell;
+    const int nx = n->nx, ny = n->ny, W = n->W, nz = n->nz;
+    const int S = B * nz;
+    const long rows = (long)S * n->ncell, slab = n->ncell * W;
     const float *bx = n->bx.as<float>(), *by = n->by.as<float>();
     EGX_CUDA(cudaMemsetAsync(n->grads.p, 0, n->n_params * sizeof(float), s));
     float *dOut = n->dOut.as<float>();
@@ -453,20 +462,30 @@ void backward(egx_net *n, int B, cudaStream_t s, long *launches) {
         gemm(ga((int)rows, W, W, 1, dPre, W, 1, 0, n->p(n->off_Wp[l]), 1, W, 0, dH2, W, 1, 0), s, launches);
         // spectral branch
         float *dS1 = n->dS1.as<float>(), *dV = n->dV.as<float>(), *dU = n->dU.as<float>(), *dU1 = n->dU1.as<float>();
-        gemm(ga(KM, W, ny, B * nx, by, 1, KM, 0, dPre, W, 1, (long)ny * W, dS1, W, 1, (long)KM * W), s, launches);
-        gemm(ga(KM, KM * W, nx, B, bx, 1, KM, 0, dS1, (long)KM * W, 1, (long)nx * KM * W, dV, (long)KM * W, 1,
+        gemm(ga(KM, W, ny, S * nx, by, 1, KM, 0, dPre, W, 1, (long)ny * W, dS1, W, 1, (long)KM * W), s, launches);
+        gemm(ga(KM, KM * W, nx, S, bx, 1, KM, 0, dS1, (long)KM * W, 1, (long)nx * KM * W, dV, (long)KM * W, 1,
                 (long)KM * KM * W),
              s, launches);
-        gemm(ga(W, W, B, KM * KM, Ul, 1, (long)KM * KM * W, W, dV, (long)KM * KM * W, 1, W, n->gr(n->off_Wm[l]), W,
+        gemm(ga(W, W, S, KM * KM, Ul, 1, (long)KM * KM * W, W, dV, (long)KM * KM * W, 1, W, n->gr(n->off_Wm[l]), W,
                 1, (long)W * W),
              s, launches);
-        gemm(ga(B, W, W, KM * KM, dV, (long)KM * KM * W, 1, W, n->p(n->off_Wm[l]), 1, W, (long)W * W, dU,
+        gemm(ga(S, W, W, KM * KM, dV, (long)KM * KM * W, 1, W, n->p(n->off_Wm[l]), 1, W, (long)W * W, dU,
                 (long)KM * KM * W, 1, W),
              s, launches);
-        gemm(ga(ny, W, KM, B * KM, by, KM, 1, 0, dU, W, 1, (long)KM * W, dU1, W, 1, (long)ny * W), s, launches);
-        gemm(ga(nx, ny * W, KM, B, bx, KM, 1, 0, dU1, (long)ny * W, 1, (long)KM * ny * W, dH2, (long)ny * W, 1,
+        gemm(ga(ny, W, KM, S * KM, by, KM, 1, 0, dU, W, 1, (long)KM * W, dU1, W, 1, (long)ny * W), s, launches);
+        gemm(ga(nx, ny * W, KM, S, bx, KM, 1, 0, dU1, (long)ny * W, 1, (long)KM * ny * W, dH2, (long)ny * W, 1,
                 (long)nx * ny * W, 1.f),
              s, launches);
+        // depth mixing: dH2[b, z'] += sum_z Dz[z, z'] dPre[b, z]; dDz[z, z'] =
+        // sum over samples and (cell, channel) of dPre[b, z] H[b, z'] (each
+        // sample's product added into the gradient)
+        gemm(ga(nz, (int)slab, nz, B, n->p(n->off_Dz[l]), 1, nz, 0, dPre, slab, 1, (long)nz * slab, dH2, slab, 1,
+                (long)nz * slab, 1.f),
+             s, launches);
+        for (int b = 0; b < B; b++)
+            gemm(wgrad(ga(nz, nz, (int)slab, 1, dPre + (long)b * nz * slab, slab, 1, 0, Hl + (long)b * nz * slab, 1,
+                          slab, 0, n->gr(n->off_Dz[l]), nz, 1, 0, 1.f)),
+                 s, launches);
         n->dH.swap(n->dH2);
     }
     // dP = X0^T dH0, dbP
@@ -485,8 +504,8 @@ void encode(egx_net *n, const float2 *v, int B, cudaStream_t s, long *launches) 
     EGX_CUDA(cudaMemsetAsync(sums, 0, B * sizeof(double), s));
     k_sample_norm2<<<dim3((unsigned)std::min<long>((N + 255) / 256, 512), B), 256, 0, s>>>(v, N, sums);
     k_rms<<<1, 64, 0, s>>>(sums, N, B, inv, rms);
-    k_encode<<<blocks_for((long)B * n->ncell * n->cin), 256, 0, s>>>(v, inv, n->logsig.as<float>(), n->ncell, n->nz, B,
-                                                                     n->X0.as<float>());
+    k_encode<<<blocks_for((long)B * n->nz * n->ncell * n->cin), 256, 0, s>>>(
+        v, inv, n->logsig.as<float>(), n->nmodels, n->ncell, n->nz, B, n->X0.as<float>());
     if (launches) *launches += 3;
 }
 
@@ -523,7 +542,7 @@ int egx_net_create(egx_ctx *ctx, int nx, int ny, int nz, int width, int layers, 
         set_device(ctx);
         auto n = std::unique_ptr<egx_net>(new egx_net());
         n->nx = nx, n->ny = ny, n->nz = nz, n->W = width, n->L = layers;
-        n->cin = 7 * nz, n->cout = 6 * nz, n->ncell = (long)nx * ny;
+        n->cin = 7, n->cout = 6, n->ncell = (long)nx * ny;
         long off = 0;
         auto take = [&](long k) {
             const long o = off;
@@ -535,6 +554,7 @@ int egx_net_create(egx_ctx *ctx, int nx, int ny, int nz, int width, int layers, 
         for (int l = 0; l < layers; l++) {
             n->off_Wm.push_back(take((long)KM * KM * width * width));
             n->off_Wp.push_back(take((long)width * width));
+            n->off_Dz.push_back(take((long)nz * nz));
             n->off_b.push_back(take(width));
         }
         n->off_Q = take((long)width * n->cout);
@@ -550,6 +570,7 @@ int egx_net_create(egx_ctx *ctx, int nx, int ny, int nz, int width, int layers, 
         for (int l = 0; l < layers; l++) {
             fill(n->off_Wm[l], (long)KM * KM * width * width, 1.f / (float)width);
             fill(n->off_Wp[l], (long)width * width, 1.f / std::sqrt((float)width));
+            fill(n->off_Dz[l], (long)nz * nz, 0.5f / std::sqrt((float)nz));
         }
         // Q = 0: the untrained network is the identity preconditioner
         n->params.ensure(off * sizeof(float));
@@ -610,16 +631,22 @@ int egx_net_params(egx_ctx *ctx, egx_net *net, float *host, int set) {
     });
 }
 
-int egx_net_set_model(egx_ctx *ctx, egx_net *net, const float *logsig) {
+int egx_net_set_models(egx_ctx *ctx, egx_net *net, const float *logsig, int count) {
     if (!ctx) return EGX_ERR_INVALID;
     EGX_GUARD(ctx, {
-        EGX_CHECK(net && logsig, EGX_ERR_INVALID, "null network or log-conductivity");
+        EGX_CHECK(net && logsig && count >= 1 && count <= 64, EGX_ERR_INVALID,
+                  "null network or log-conductivity, or count outside 1..64");
         set_device(ctx);
-        const size_t bytes = (size_t)net->ncell * net->nz * sizeof(float);
+        const size_t bytes = (size_t)count * net->ncell * net->nz * sizeof(float);
         net->logsig.ensure(bytes);
         EGX_CUDA(cudaMemcpyAsync(net->logsig.p, logsig, bytes, cudaMemcpyHostToDevice, ctx->stream));
         EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+        net->nmodels = count;
     });
+}
+
+int egx_net_set_model(egx_ctx *ctx, egx_net *net, const float *logsig) {
+    return egx_net_set_models(ctx, net, logsig, 1);
 }
 
 int egx_net_loss_grad(egx_ctx *ctx, egx_net *net, const float *v, const float *t, int batch, float *loss, float *grad,
@@ -648,10 +675,10 @@ int egx_net_loss_grad(egx_ctx *ctx, egx_net *net, const float *v, const float *t
         ensure_batch(net, batch);
         encode(net, dv, batch, s, &ctx->launches);
         const float *inv = net->scal.as<float>();
-        k_encode_target<<<blocks_for((long)batch * net->ncell * net->cout), 256, 0, s>>>(dt, inv, net->ncell, net->nz,
+        k_encode_target<<<blocks_for((long)batch * net->nz * net->ncell * net->cout), 256, 0, s>>>(dt, inv, net->ncell, net->nz,
                                                                                          batch, net->T.as<float>());
         forward(net, batch, s, &ctx->launches);
-        const long per = net->ncell * net->cout;
+        const long per = (long)net->nz * net->ncell * net->cout;  // one sample's outputs
         double *e2 = net->sums.as<double>() + batch, *t2 = e2 + batch;
         EGX_CUDA(cudaMemsetAsync(e2, 0, 2 * batch * sizeof(double), s));
         k_loss_sums<<<dim3((unsigned)std::min<long>((per + 255) / 256, 512), batch), 256, 0, s>>>(

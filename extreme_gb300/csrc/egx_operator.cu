@@ -248,10 +248,10 @@ static void launch_reg(int which, cudaStream_t s, int nlines, const C<T> *x, con
 template <typename T, int N>
 static void launch_reg_tile(int which, cudaStream_t s, int nlines, const C<T> *x, const OperatorData<T> *op,
                             C<T> *buf, C<T> *y, const OpDims *d, long lstride, long estride, int B, int nload,
-                            int nstore, const C<T> *tw, int sign) {
+                            int nstore, const C<T> *tw, int sign, int tile) {
     // 64-byte tiles for the y passes and for x passes that write more rows
-    // than they read; 128-byte tiles otherwise
-    if (which != 1 || nload < nstore)
+    // than they read; 128-byte tiles otherwise (unless the tuner chose)
+    if (tile == 1 || (tile == 0 && (which != 1 || nload < nstore)))
         launch_reg<T, N, RegCols<T>::BTN>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw,
                                            sign);
     else
@@ -263,13 +263,13 @@ static void launch_reg_tile(int which, cudaStream_t s, int nlines, const C<T> *x
 template <typename T>
 static bool run_reg(int n, int which, int nlines, int B, cudaStream_t s, const C<T> *x, const OperatorData<T> *op,
                     C<T> *buf, C<T> *y, const OpDims *d, long lstride, long estride, int nload, int nstore,
-                    const C<T> *tw, int sign) {
+                    const C<T> *tw, int sign, int tile = 0) {
     if (!reg_fft_ok(n)) return false;
     switch (n) {
-        case 64: launch_reg_tile<T, 64>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
-        case 128: launch_reg_tile<T, 128>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
-        case 256: launch_reg_tile<T, 256>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
-        default: launch_reg_tile<T, 512>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign); break;
+        case 64: launch_reg_tile<T, 64>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign, tile); break;
+        case 128: launch_reg_tile<T, 128>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign, tile); break;
+        case 256: launch_reg_tile<T, 256>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign, tile); break;
+        default: launch_reg_tile<T, 512>(which, s, nlines, x, op, buf, y, d, lstride, estride, B, nload, nstore, tw, sign, tile); break;
     }
     return true;
 }
@@ -494,7 +494,7 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
     // 1. r*x, forward factors, zero padding, DFT along y (rows i < nx)
     {
         ev = tm ? tm->begin(EGX_K_FWD_Y + koff, s) : -1;
-        if (!run_reg<T>(n1, 0, d.nx, d.B, s, x, &op, buf, nullptr, &d, 0, 0, 0, 0, tw1, -1)) {
+        if (!run_reg<T>(n1, 0, d.nx, d.B, s, x, &op, buf, nullptr, &d, 0, 0, 0, 0, tw1, -1, d.fft_tile)) {
             int bt = fft_cols(n1, sizeof(C<T>));
             size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
             set_smem<T>((const void *)k_fwd_y<T>, sm);
@@ -507,7 +507,7 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
     {
         ev = tm ? tm->begin(EGX_K_FWD_X + koff, s) : -1;
         if (!run_reg<T>(n0, 1, n1, d.B, s, nullptr, nullptr, buf, nullptr, nullptr, d.B, (long)n1 * d.B, d.nx, n0,
-                        tw0, -1)) {
+                        tw0, -1, d.fft_tile)) {
             int bt = fft_cols(n0, sizeof(C<T>));
             size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
             set_smem<T>((const void *)k_lines<T>, sm);
@@ -531,9 +531,9 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
             launch_contract_sb(reinterpret_cast<float2 *>(buf), reinterpret_cast<const float2 *>(G), d, err, s,
                                &extra);
             if (launches) *launches += extra - 1;
-        } else if (std::is_same<T, float>::value && err && contract_mma_fits(d.nz, d.nrhs)) {
+        } else if (std::is_same<T, float>::value && err && d.contract_variant == 0 && contract_mma_fits(d.nz, d.nrhs)) {
             launch_contract_mma(reinterpret_cast<float2 *>(buf), reinterpret_cast<const float2 *>(G), d, err, s);
-        } else if (std::is_same<T, float>::value && err && contract_c64_fits(d.nz, d.nrhs)) {
+        } else if (std::is_same<T, float>::value && err && d.contract_variant != 2 && contract_c64_fits(d.nz, d.nrhs)) {
             launch_contract_c64(reinterpret_cast<float2 *>(buf), reinterpret_cast<const float2 *>(G), d, err, s);
         } else if (std::is_same<T, double>::value && d.ds && contract_ds_fits(d.nz, d.nrhs)) {
             const int per = 3 * d.nz;
@@ -554,7 +554,7 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
     {
         ev = tm ? tm->begin(EGX_K_BWD_X + koff, s) : -1;
         if (!run_reg<T>(n0, 1, n1, d.B, s, nullptr, nullptr, buf, nullptr, nullptr, d.B, (long)n1 * d.B, n0, d.nx,
-                        tw0, +1)) {
+                        tw0, +1, d.fft_tile)) {
             int bt = fft_cols(n0, sizeof(C<T>));
             size_t sm = 2 * (size_t)n0 * bt * sizeof(C<T>);
             set_smem<T>((const void *)k_lines<T>, sm);
@@ -567,7 +567,7 @@ void operator_apply(const OpDims &d, const OperatorData<T> &op, const C<T> *G, c
     // 5. inverse DFT along y, extraction, last step
     {
         ev = tm ? tm->begin(EGX_K_BWD_Y + koff, s) : -1;
-        if (!run_reg<T>(n1, 2, d.nx, d.B, s, x, &op, buf, y, &d, 0, 0, 0, 0, tw1, +1)) {
+        if (!run_reg<T>(n1, 2, d.nx, d.B, s, x, &op, buf, y, &d, 0, 0, 0, 0, tw1, +1, d.fft_tile)) {
             int bt = fft_cols(n1, sizeof(C<T>));
             size_t sm = 2 * (size_t)n1 * bt * sizeof(C<T>);
             set_smem<T>((const void *)k_bwd_y<T>, sm);

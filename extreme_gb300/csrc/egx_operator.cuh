@@ -29,6 +29,13 @@ struct OpDims {
     int B;       // batch of the spectral buffer: nrhs * 3 * nz
     long nvec;   // elements of one anomaly vector: nx*ny*3*nz
     int ds = 0;  // complex128 apply: contraction in double-FP32 arithmetic
+    // kernel variants chosen by the apply tuner (egx_tune_apply): FFT
+    // column tile of the register passes (0 the built-in choice per pass,
+    // 1 64-byte tiles, 2 128-byte tiles) and the complex64 contraction of
+    // the packed Green layout (0 the built-in order, 1 the TMA-staged
+    // CUDA-core kernel, 2 the generic kernel)
+    int fft_tile = 0;
+    int contract_variant = 0;
 };
 
 template <typename T>

@@ -22,14 +22,14 @@ PRECOND_GMRES, PRECOND_CALLBACK, PRECOND_NONE, PRECOND_LEARNED = 0, 1, 2, 3
 # Every symbol the header declares (checked by the ABI test).
 EXPORTS = [
     "egx_create", "egx_destroy", "egx_last_error", "egx_version", "egx_device_allocations", "egx_set_stream",
-    "egx_launch_count",
+    "egx_launch_count", "egx_set_graphs", "egx_graph_stats", "egx_tune_apply", "egx_apply_variant",
     "egx_green_build", "egx_green_upload", "egx_green_download", "egx_green_free",
     "egx_op_prepare", "egx_op_apply", "egx_op_apply_ds", "egx_op_apply_c64", "egx_fft2d",
     "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products", "egx_dot_products_static",
     "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_kinds",
     "egx_profile_read",
     "egx_level_fields", "egx_level_cache", "egx_set_level_precision", "egx_mt_responses", "egx_wait_selftest",
-    "egx_net_create", "egx_net_free", "egx_net_size", "egx_net_params", "egx_net_set_model", "egx_net_loss_grad",
+    "egx_net_create", "egx_net_free", "egx_net_size", "egx_net_params", "egx_net_set_model", "egx_net_set_models", "egx_net_loss_grad",
     "egx_net_adam", "egx_net_apply", "egx_learned_stats", "egx_learned_inject_nonfinite",
 ]
 
@@ -99,6 +99,10 @@ def load(path=None):
     lib.egx_set_stream.argtypes = [vp, vp]
     lib.egx_launch_count.argtypes = [vp]
     lib.egx_launch_count.restype = C.c_long
+    lib.egx_set_graphs.argtypes = [vp, i]
+    lib.egx_tune_apply.argtypes = [vp, i, i, vp]
+    lib.egx_apply_variant.argtypes = [vp, i, i]
+    lib.egx_graph_stats.argtypes = [vp, C.POINTER(C.c_long), C.POINTER(C.c_long)]
     lib.egx_device_allocations.argtypes = []
     lib.egx_device_allocations.restype = C.c_long
     lib.egx_green_build.argtypes = [vp, C.POINTER(Model), d, i, i, C.POINTER(vp)]
@@ -130,6 +134,7 @@ def load(path=None):
     lib.egx_net_size.restype = C.c_long
     lib.egx_net_params.argtypes = [vp, vp, vp, i]
     lib.egx_net_set_model.argtypes = [vp, vp, vp]
+    lib.egx_net_set_models.argtypes = [vp, vp, vp, i]
     lib.egx_net_loss_grad.argtypes = [vp, vp, vp, vp, i, C.POINTER(C.c_float), vp, i]
     lib.egx_net_adam.argtypes = [vp, vp, C.c_float]
     lib.egx_net_apply.argtypes = [vp, vp, vp, vp, i, i]
@@ -187,6 +192,28 @@ class Context:
 
     def launch_count(self):
         return int(self.lib.egx_launch_count(self.h))
+
+    def set_graphs(self, enable):
+        """Capture the inner GMRES cycle as a CUDA graph and replay it (egx_set_graphs)."""
+        self._check(self.lib.egx_set_graphs(self.h, int(bool(enable))))
+
+    def tune_apply(self, nrhs=2, reps=5):
+        """egx_tune_apply: times every (FFT tile, contraction kernel) variant
+        of the complex64 apply; keeps the fastest. Returns (tile, variant,
+        {(tile, variant): ms})."""
+        ms = np.zeros(9)
+        self._check(self.lib.egx_tune_apply(self.h, nrhs, reps, _ptr(ms)))
+        table = {(t, v): float(ms[3 * t + v]) for t in range(3) for v in range(3) if ms[3 * t + v] >= 0}
+        best = min(table, key=table.get)
+        return best[0], best[1], table
+
+    def apply_variant(self, fft_tile=0, contract_variant=0):
+        self._check(self.lib.egx_apply_variant(self.h, fft_tile, contract_variant))
+
+    def graph_stats(self):
+        r, nn = C.c_long(), C.c_long()
+        self._check(self.lib.egx_graph_stats(self.h, C.byref(r), C.byref(nn)))
+        return r.value, nn.value
 
     @staticmethod
     def device_allocations():
@@ -460,10 +487,15 @@ class SpectralNet:
         self.ctx._check(self.ctx.lib.egx_net_params(self.ctx.h, self.h, _ptr(v), 1))
 
     def set_model(self, logsig):
-        """log10(omega mu0 sigma dx dy) per anomaly cell, [nx, ny, nz]."""
+        """log10(omega mu0 sigma dx dy) per anomaly cell, [nx, ny, nz], or
+        [count, nx, ny, nz] for a batch whose sample b uses model b % count."""
         ls = np.ascontiguousarray(logsig, np.float32)
-        assert ls.shape == (self.nx, self.ny, self.nz)
-        self.ctx._check(self.ctx.lib.egx_net_set_model(self.ctx.h, self.h, _ptr(ls)))
+        if ls.ndim == 3:
+            assert ls.shape == (self.nx, self.ny, self.nz)
+            self.ctx._check(self.ctx.lib.egx_net_set_model(self.ctx.h, self.h, _ptr(ls)))
+        else:
+            assert ls.shape[1:] == (self.nx, self.ny, self.nz)
+            self.ctx._check(self.ctx.lib.egx_net_set_models(self.ctx.h, self.h, _ptr(ls), ls.shape[0]))
 
     def loss_grad(self, v, t, want_grad=False):
         """Loss (and the flat gradient) for residuals v and target corrections

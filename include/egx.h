@@ -120,6 +120,29 @@ int egx_version(void);
 long egx_device_allocations(void);
 /* Use an external CUDA stream (cudaStream_t) for all work of this context. */
 int egx_set_stream(egx_ctx *ctx, void *stream);
+/* Execution of the flexible preconditioner (no reference counterpart; the
+ * arithmetic is unchanged). The Arnoldi decisions of every solve run on the
+ * device; with enable != 0 the inner GMRES cycle of each outer FGMRES step
+ * is additionally captured once as a CUDA graph (per prepared operator,
+ * tolerance and buffer set) and replayed, one launch instead of a few
+ * hundred -- for many small solves, where launching is the cost. Ignored
+ * while per-kernel timing (egx_profile) is on. Default off. */
+int egx_set_graphs(egx_ctx *ctx, int enable);
+/* Replays of the captured inner cycle since the context was created and the
+ * kernel nodes of the last capture. */
+int egx_graph_stats(egx_ctx *ctx, long *replays, long *nodes);
+/* Apply autotuner (no reference counterpart): on the prepared operator
+ * (complex64 Green tensor), times `reps` complex64 applies of nrhs vectors
+ * for every kernel variant -- the FFT passes' column tile (0 built-in per
+ * pass, 1 64-byte, 2 128-byte) x the contraction kernel of the packed Green
+ * layout (0 built-in order, 1 TMA-staged CUDA-core, 2 generic; the sub-block
+ * layout of nz in {16, 32, 48} has one) -- keeps the fastest for the
+ * context's later complex64 applies, and writes the mean ms per apply to
+ * ms_out[tile * 3 + variant] (9 doubles, -1 where not applicable; may be
+ * NULL). The results do not depend on the choice. */
+int egx_tune_apply(egx_ctx *ctx, int nrhs, int reps, double *ms_out);
+/* Set the variants by hand (same ranges). */
+int egx_apply_variant(egx_ctx *ctx, int fft_tile, int contract_variant);
 /* Count of this library's kernel launches since the context was created. */
 long egx_launch_count(egx_ctx *ctx);
 
@@ -182,37 +205,43 @@ int egx_set_precond(egx_ctx *ctx, int kind, egx_precond_fn fn, void *user);
 
 /* ---- learned flexible preconditioner (the RightPreconditionerRequest plug
  * point, FlexibleGmresSolver.cs:24-36; no reference counterpart otherwise) --
- * A spectral network on the lateral grid proposes the correction z - v,
- * z ~ A^-1 v, from the residual v and the log-conductivity:
- * z = v + rms(v) N(v / rms(v)). Input per lateral cell: Re, Im of the three
- * residual components and log10(omega mu0 sigma dx dy) of every anomaly
- * layer; `layers` spectral layers of `width` channels, 16 x 16 lateral modes
- * (real Fourier basis), GELU; BF16 tensor-core GEMMs with FP32 accumulation
- * for the forward and backward passes, Adam. Vectors are complex64 [batch][N]
- * in the anomaly layout; batch <= 64. The output layer starts at zero: an
- * untrained network is the identity. */
+ * A spectral network z = N(v) = v + rms(v) Out(v / rms(v), log sigma) on the
+ * nx x ny x nz anomaly mesh, depth a spatial axis: 7 input channels per cell
+ * (Re and Im of the three residual components, log10(omega mu0 sigma dx dy)),
+ * a lift to `width` channels, `layers` layers each of a per-depth lateral
+ * spectral convolution (16 x 16 retained modes in a real Fourier basis, a
+ * width x width mixing per mode), a pointwise width x width map and an
+ * nz x nz depth mixing, GELU between layers, a projection to 6 channels
+ * (Re and Im of the correction) that starts at zero: an untrained network
+ * is the identity. BF16 tensor-core GEMMs with FP32 accumulation for the
+ * forward and backward passes, Adam. Vectors are complex64 [batch][N] in the
+ * anomaly layout; batch <= 64. */
 int egx_net_create(egx_ctx *ctx, int nx, int ny, int nz, int width, int layers, unsigned seed, egx_net **out);
 int egx_net_free(egx_ctx *ctx, egx_net *net);
 long egx_net_size(const egx_net *net);                               /* parameters */
 int egx_net_params(egx_ctx *ctx, egx_net *net, float *host, int set);  /* set = 0 read, 1 write */
 /* log-conductivity channel, [nx][ny][nz] host floats */
 int egx_net_set_model(egx_ctx *ctx, egx_net *net, const float *logsig);
+/* `count` log-conductivity models [count][nx][ny][nz] (1..64): sample b of
+ * the next calls uses model b % count (training batches drawn from several
+ * solves) */
+int egx_net_set_models(egx_ctx *ctx, egx_net *net, const float *logsig, int count);
 /* loss = mean_b |N(v_b/rms_b) - t_b/rms_b|^2 / |t_b/rms_b|^2 for targets t = z* - v;
  * gradients kept for egx_net_adam and copied to grad (n_params floats) if not NULL */
 int egx_net_loss_grad(egx_ctx *ctx, egx_net *net, const float *v, const float *t, int batch, float *loss, float *grad,
                       int where);
 int egx_net_adam(egx_ctx *ctx, egx_net *net, float lr);
 int egx_net_apply(egx_ctx *ctx, egx_net *net, const float *v, float *z, int batch, int where);
-/* With egx_set_precond(ctx, EGX_PRECOND_LEARNED, NULL, net) the inner solves
- * of the mixed form are FGMRES whose flexible preconditioner is the
- * reference's inner GMRES(m_in) cycle started from the network's estimate
- * v + rms(v) N(v/rms(v)) of A^-1 v instead of from v
- * (FlexibleGmresWithGmresPreconditioner.cs:35-44); the network must be built
- * for the solve's grid (EGX_ERR_INVALID otherwise). An inner solve that does
- * not reach its tolerance is redone with the GMRES preconditioner (the
- * fallback), and the refinement's complex128 residual judges the result.
- * uses/fallbacks count the inner solves since the context was created.
- * EGX_PRECOND_NONE makes the mixed form's inner FGMRES unpreconditioned. */
+/* With egx_set_precond(ctx, EGX_PRECOND_LEARNED, NULL, net) each inner
+ * complex64 FGMRES of the mixed form uses the network as its flexible right
+ * preconditioner, z_j = N(v_j), in place of the reference's inner GMRES(m_in)
+ * cycle (FlexibleGmresWithGmresPreconditioner.cs:35-57); the network must be
+ * built for the solve's grid (EGX_ERR_INVALID otherwise). An inner solve that
+ * does not reach its tolerance within min(inner_restarts, 4) cycles is redone
+ * with the GMRES preconditioner (the fallback), and the refinement's
+ * complex128 residual judges the result. uses/fallbacks count the inner
+ * solves since the context was created. EGX_PRECOND_NONE makes the mixed
+ * form's inner FGMRES unpreconditioned. */
 int egx_learned_stats(egx_ctx *ctx, long *uses, long *fallbacks);
 /* Failure-injection hook for tests (no reference counterpart): the next
  * `count` applications of the learned preconditioner have the first entry of

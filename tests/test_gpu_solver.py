@@ -91,3 +91,29 @@ def test_mixed_solve_small(egx_ctx, small_solve):
     assert res < 1e-6
     assert rel(x, out.chi) < 1e-5
     g.free()
+
+
+@pytest.mark.parametrize("precision", [egx.PREC_FP64, egx.PREC_MIXED])
+def test_device_krylov_control_matches_host_driver(egx_ctx, small_solve, precision, monkeypatch):
+    """The Arnoldi decisions taken on the device (default) and by the host
+    driver (EGX_KRYLOV_HOST=1) give the same iteration counts, apply counts
+    and solutions (complex128: to 1e-12; the mixed form, whose complex64
+    inner vectors can round differently when a coefficient differs in its
+    last bit: both to their 1e-6 target, jQ within 2e-6)."""
+    from extreme_gb300.forward import ForwardSettings, MixedSettings, Mt3DForwardSolver
+    m, om, G, out = small_solve
+    solver = Mt3DForwardSolver(ForwardSettings(residual=1e-8, outer_buffer_length=20), precision=precision,
+                               mixed=MixedSettings(tol=1e-6), ctx=egx_ctx)
+    sols = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("EGX_KRYLOV_HOST", mode)
+        sols[mode] = solver.solve(m, 0.1)
+    a, b = sols["0"], sols["1"]
+    for i in range(2):
+        if precision == egx.PREC_FP64:
+            assert a.results[i]["iterations"] == b.results[i]["iterations"]
+            assert a.results[i]["n_applies"] == b.results[i]["n_applies"]
+            assert rel(a.jq[i], b.jq[i]) < 1e-12
+        else:
+            assert a.results[i]["true_be"] < 1e-6 and b.results[i]["true_be"] < 1e-6
+            assert rel(a.jq[i], b.jq[i]) < 2e-6
