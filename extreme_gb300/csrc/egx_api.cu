@@ -131,7 +131,7 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
         outer->reset();
         inner->reset();
         outer->reset(new Gmres<T>(n, m_out, tol, max_restarts, check_true, ctx->stream));
-        if (precond_kind == EGX_PRECOND_GMRES || precond_kind == EGX_PRECOND_LEARNED) {
+        if (precond_kind == EGX_PRECOND_GMRES) {
             inner->reset(new Gmres<T>(n, m_in, tol, 1, false, ctx->stream));
             // the inner cycle is enqueued whole: its steps never wait for the host
             (*inner)->enqueue_only = true;
@@ -212,14 +212,12 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
         }
     } else if (precond_kind == EGX_PRECOND_LEARNED) {
         EGX_CHECK(!dbl && ctx->precond_user, EGX_ERR_STATE, "learned preconditioner without a network");
-        // the network's estimate of A^-1 v starts the inner GMRES cycle in
-        // place of v itself (x0 = v in FlexibleGmresWithGmresPreconditioner.cs:35-44)
+        // the network is the flexible right preconditioner, z_j = N(v_j), in
+        // place of the inner GMRES(m_in) cycle
+        // (FlexibleGmresWithGmresPreconditioner.cs:35-57)
         egx_net *net = static_cast<egx_net *>(ctx->precond_user);
         EGX_CHECK(net_length(net) == nvec(ctx), EGX_ERR_INVALID, "learned preconditioner built for another grid");
-        (*inner)->apply = apply_inner;
-        (*inner)->timers = &ctx->timers;
-        Gmres<T> *in = inner->get();
-        (*outer)->precond = [ctx, net, nrhs, in](const C<T> *src, C<T> *dst) {
+        (*outer)->precond = [ctx, net, nrhs](const C<T> *src, C<T> *dst) {
             net_apply(net, reinterpret_cast<const float2 *>(src), reinterpret_cast<float2 *>(dst), nrhs, ctx->stream,
                       &ctx->launches);
             if (ctx->learned_inject > 0) {
@@ -229,7 +227,6 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
                 ctx->learned_inject--;
                 EGX_CUDA(cudaMemcpyAsync(dst, &kNonFinite, sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
             }
-            in->solve(src, dst, dst);
         };
     } else if (precond_kind == EGX_PRECOND_CALLBACK) {
         egx_precond_fn fn = ctx->precond_fn;
@@ -487,11 +484,11 @@ GmresResult mixed_dev(egx_ctx *ctx, const double2 *b, double2 *x, const egx_mixe
         GmresResult ir;
         bool done = false;
         if (ctx->precond_kind == EGX_PRECOND_LEARNED) {
-            // the network as the flexible preconditioner, with the inner
-            // solve's restart budget; then the GMRES-preconditioned solve
-            // from zero (the fallback)
+            // the network as the flexible preconditioner, at most four
+            // FGMRES cycles; then the GMRES-preconditioned solve from zero
+            // (the fallback)
             ctx->learned_uses++;
-            ir = run_fgmres<float>(ctx, r32, d32, p.m_out, p.m_in, itol, p.inner_restarts, false,
+            ir = run_fgmres<float>(ctx, r32, d32, p.m_out, p.m_in, itol, std::min(p.inner_restarts, 4), false,
                                    EGX_PRECOND_LEARNED, &a32, nrhs);
             done = ir.converged;
             if (!done) {

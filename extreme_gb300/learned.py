@@ -1,19 +1,20 @@
 """Learned flexible preconditioner: data, training and evaluation around the
 library's network (``egx_net_*``).
 
-* ``collect_pairs`` -- (residual, correction) pairs that the solver itself
-  generates: the residuals v are the orthonormal Arnoldi vectors of the
-  operator A on the right-hand sides chi0 of both polarisations, the targets
-  t = A^-1 v - v (FP64 FGMRES to 1e-8), all through the library on the
-  device. In the solve the network's v + N(v) starts the reference's inner
-  GMRES(m_in) cycle in place of x0 = v
-  (``FlexibleGmresWithGmresPreconditioner.cs:35-57``).
+* ``collect_pairs`` -- (residual, GMRES-preconditioner correction) pairs that
+  the solver itself generates: the residuals v are orthonormal Arnoldi
+  vectors of the operator A on the right-hand sides chi0 of both
+  polarisations (the vectors the outer FGMRES hands its preconditioner), the
+  targets t = M(v) - v with M the reference's inner preconditioner -- one
+  GMRES(m_in) cycle from x0 = v (``FlexibleGmresWithGmresPreconditioner.cs:35-57``)
+  -- all through the library on the device.
 * ``train`` -- Adam on the GPU through ``egx_net_loss_grad`` /
-  ``egx_net_adam`` (BF16 tensor-core forward and backward kernels).
+  ``egx_net_adam`` (BF16 tensor-core forward and backward kernels), each
+  batch drawn across solves with their own conductivity channels.
 * ``evaluate`` -- held-out solves of the mixed form with the GMRES
   preconditioner (the reference's method), without a preconditioner, and with
-  the network (GMRES as fallback, the FP64 residual as judge): iterations,
-  operator applies, fallbacks, wall time.
+  the network as the flexible preconditioner (GMRES as fallback, the FP64
+  residual as judge): iterations, operator applies, fallbacks, wall time.
 
 torch holds the device buffers (vectors of the pairs); it is plumbing.
 """
@@ -36,14 +37,17 @@ def log_conductivity(model: CartesianModel, frequency: float):
 
 @dataclass
 class PairSet:
-    """Pairs of one (model, frequency) on the device: v [k, N], t = z - v [k, N]
-    (complex64), and the conductivity channel [nx, ny, nz]."""
+    """Pairs of one (model, frequency) on the device: v [k, N], t = M(v) - v
+    [k, N] (complex64), and the conductivity channel [nx, ny, nz]."""
     v: object
     t: object
     logsig: np.ndarray
 
 
-def collect_pairs(ctx: egx.Context, model: CartesianModel, frequency: float, n_vectors=12, tol=1e-8) -> PairSet:
+def collect_pairs(ctx: egx.Context, model: CartesianModel, frequency: float, n_vectors=4, m_in=10, tol=1e-7,
+                  pols=(0, 1)) -> PairSet:
+    """n_vectors Arnoldi vectors per polarisation in ``pols`` and their
+    GMRES(m_in) preconditioner outputs."""
     import torch
     omega = freq_to_omega(frequency)
     zeta, zeta0 = model_zeta(model, omega)
@@ -53,7 +57,7 @@ def collect_pairs(ctx: egx.Context, model: CartesianModel, frequency: float, n_v
     try:
         rhs = []
         ctx.op_prepare(g, zeta, zeta0, model.layer_thickness, egx.OP_CHI0)
-        for pol in (0, 1):
+        for pol in pols:
             js = np.zeros((model.nx, model.ny, 3, model.nz), complex)
             js[:, :, pol, :] = (zeta - zeta0[None, None, :]) * e0[None, None, :]
             rhs.append(torch.tensor(ctx.op_apply(js.reshape(-1)), device=dev))
@@ -71,14 +75,13 @@ def collect_pairs(ctx: egx.Context, model: CartesianModel, frequency: float, n_v
             V = [b / torch.linalg.norm(b)]
             for j in range(n_vectors):
                 v = V[-1]
-                x = v.clone()
+                z = v.clone()
                 torch.cuda.synchronize()
-                r = ctx.fgmres_solve_dev(v.data_ptr(), x.data_ptr(), m_out=15, m_in=10, tol=tol, max_restarts=100,
-                                         precond=egx.PRECOND_GMRES, check_true=False)
-                if not r["converged"]:
-                    raise RuntimeError("target solve did not converge")
+                # the inner preconditioner: one GMRES(m_in) cycle from x0 = v
+                ctx.fgmres_solve_dev(v.data_ptr(), z.data_ptr(), m_out=m_in, m_in=1, tol=tol, max_restarts=1,
+                                     precond=egx.PRECOND_NONE, check_true=False)
                 vs.append(v.to(torch.complex64))
-                ts.append((x - v).to(torch.complex64))
+                ts.append((z - v).to(torch.complex64))
                 if j == n_vectors - 1:
                     break
                 w = A(v)
@@ -97,19 +100,18 @@ class TrainLog:
 
 
 def train(net: egx.SpectralNet, sets: List[PairSet], steps=500, batch=8, lr=1e-3, seed=0) -> TrainLog:
-    """Adam on random batches drawn from one (model, frequency) set at a time
-    (the conductivity channel belongs to the set)."""
+    """Adam on random batches of pairs drawn across the sets; every sample
+    carries its own set's conductivity channel."""
     import torch
     rng = np.random.default_rng(seed)
     log = TrainLog()
     t0 = time.perf_counter()
+    index = [(i, j) for i, s in enumerate(sets) for j in range(s.v.shape[0])]
     for step in range(steps):
-        s = sets[rng.integers(len(sets))]
-        k = s.v.shape[0]
-        idx = torch.tensor(rng.choice(k, min(batch, k), replace=False), device=s.v.device)
-        v = s.v[idx].contiguous()
-        t = s.t[idx].contiguous()
-        net.set_model(s.logsig)
+        pick = [index[k] for k in rng.choice(len(index), min(batch, len(index)), replace=False)]
+        v = torch.stack([sets[i].v[j] for i, j in pick]).contiguous()
+        t = torch.stack([sets[i].t[j] for i, j in pick]).contiguous()
+        net.set_model(np.stack([sets[i].logsig for i, _ in pick]))
         torch.cuda.synchronize()
         log.losses.append(net.loss_grad_dev(v.data_ptr(), t.data_ptr(), v.shape[0]))
         net.adam(lr)
@@ -179,34 +181,44 @@ def mean_loss(net: egx.SpectralNet, sets: List[PairSet], batch=8) -> float:
 
 
 def main(argv=None):
-    """Train on seeded random models, evaluate on held-out ones; one JSON line
-    per training chunk and per (model, frequency, method)."""
+    """Train on pairs from seeded random models at log-spaced frequencies,
+    evaluate on held-out seeds; one JSON line per training chunk and per
+    (model, frequency, method)."""
     import argparse
     import json
     from .model import scaled_model
     ap = argparse.ArgumentParser(description=main.__doc__)
-    ap.add_argument("--mesh", type=int, nargs=3, default=[64, 64, 16])
-    ap.add_argument("--train-models", type=int, default=16)
+    ap.add_argument("--mesh", type=int, nargs=3, default=[128, 128, 32])
+    ap.add_argument("--train-models", type=int, default=500)
+    ap.add_argument("--train-freqs", type=int, default=4, help="frequencies per training model, 1e-3..10 Hz")
+    ap.add_argument("--vectors", type=int, default=1, help="Arnoldi vectors per solve (alternating polarisation)")
     ap.add_argument("--held-out", type=int, nargs="+", default=[31, 32])
-    ap.add_argument("--freqs", type=float, nargs="+", default=[0.1, 1.0])
-    ap.add_argument("--width", type=int, default=16)
-    ap.add_argument("--layers", type=int, default=3)
-    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--freqs", type=float, nargs="+", default=[0.01, 1.0])
+    ap.add_argument("--width", type=int, default=32)
+    ap.add_argument("--layers", type=int, default=4)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
     a = ap.parse_args(argv)
     nx, ny, nz = a.mesh
     ctx = egx.Context(0)
     t0 = time.perf_counter()
-    sets = [collect_pairs(ctx, scaled_model(nx, ny, nz, seed=100 + s), f)
-            for s in range(a.train_models) for f in a.freqs]
-    held = [collect_pairs(ctx, scaled_model(nx, ny, nz, seed=s), f) for s in a.held_out for f in a.freqs]
-    print(json.dumps({"pairs": sum(s.v.shape[0] for s in sets), "held_pairs": sum(s.v.shape[0] for s in held),
+    rng = np.random.default_rng(2024)
+    sets = []
+    for s in range(a.train_models):
+        m = scaled_model(nx, ny, nz, seed=1000 + s)
+        for f in np.logspace(-3, 1, a.train_freqs) * 10 ** rng.uniform(-0.25, 0.25):
+            sets.append(collect_pairs(ctx, m, float(f), n_vectors=a.vectors, pols=(len(sets) % 2,)))
+    held = [collect_pairs(ctx, scaled_model(nx, ny, nz, seed=s), f, n_vectors=2) for s in a.held_out for f in a.freqs]
+    print(json.dumps({"solves": len(sets), "pairs": sum(s.v.shape[0] for s in sets),
+                      "held_pairs": sum(s.v.shape[0] for s in held),
                       "seconds": round(time.perf_counter() - t0, 1)}), flush=True)
     net = egx.SpectralNet(ctx, nx, ny, nz, width=a.width, layers=a.layers, seed=0)
+    print(json.dumps({"parameters": net.size, "held_loss_untrained": mean_loss(net, held)}), flush=True)
     chunks = 8
     for c in range(chunks):   # cosine schedule in 8 chunks
         lr = a.lr * 0.5 * (1 + np.cos(np.pi * c / chunks))
-        log = train(net, sets, steps=a.steps // chunks, lr=lr, seed=c)
+        log = train(net, sets, steps=a.steps // chunks, batch=a.batch, lr=lr, seed=c)
         print(json.dumps({"chunk": c, "lr": lr, "train_loss": float(np.mean(log.losses[-50:])),
                           "held_loss": mean_loss(net, held), "seconds": round(log.seconds, 2)}), flush=True)
     for s in a.held_out:

@@ -50,11 +50,15 @@ def _inputs(nx, ny, nz, B, seed):
     return v, t, logsig
 
 
-@pytest.mark.parametrize("nx,ny,nz,W,L,B", [(12, 10, 2, 16, 2, 2), (32, 24, 4, 32, 3, 3)])
-def test_loss_and_gradient_match_oracle(ctx, nx, ny, nz, W, L, B):
+@pytest.mark.parametrize("nx,ny,nz,W,L,B,models", [(12, 10, 2, 16, 2, 2, 1), (32, 24, 4, 32, 3, 3, 1),
+                                                   (16, 12, 5, 32, 4, 4, 4)])
+def test_loss_and_gradient_match_oracle(ctx, nx, ny, nz, W, L, B, models):
     net, flat, lay = _net(ctx, nx, ny, nz, W, L, seed=nx)
     try:
         v, t, logsig = _inputs(nx, ny, nz, B, seed=nx)
+        if models > 1:  # one conductivity model per sample (training batches across solves)
+            rng = np.random.default_rng(nx + 7)
+            logsig = rng.uniform(-3, 1, (models, nx, ny, nz)).astype(np.float32)
         net.set_model(logsig)
         loss, g = net.loss_grad(v, t, want_grad=True)
         ref_loss, ref_g = sn.loss_grad(flat, v.astype(np.complex128), t.astype(np.complex128),
@@ -135,35 +139,34 @@ def test_net_arguments_are_checked(ctx):
 
 
 def test_mixed_solve_with_learned_preconditioner(ctx):
-    """Pairs from the solver on one model, a short training run, then the
-    three inner preconditioners on a held-out model. The network's estimate
-    only seeds the reference's inner GMRES cycle, so the learned solve keeps
-    the default method's apply count per outer iteration and reaches the 1e-6
-    target; the iteration counts of the three are printed (what the network
-    gains or loses)."""
+    """Pairs (Arnoldi vector, GMRES(10) preconditioner output) from the
+    solver on one model, a short training run that lowers their loss, then
+    the mixed solve of a held-out model with the network as the flexible
+    preconditioner: whatever the network's quality, the solve reaches the
+    1e-6 target (the GMRES preconditioner takes over for an inner solve the
+    network does not finish in four cycles), and the reference's method is
+    unchanged beside it."""
     from extreme_gb300 import egx, learned
-    from extreme_gb300.forward import MixedSettings
     from extreme_gb300.model import scaled_model
     nx, ny, nz = 24, 24, 4
     f = 1.0
-    sets = [learned.collect_pairs(ctx, scaled_model(nx, ny, nz, seed=11), f, n_vectors=6)]
-    assert sets[0].v.shape == (12, nx * ny * 3 * nz)
-    held = [learned.collect_pairs(ctx, scaled_model(nx, ny, nz, seed=12), f, n_vectors=6)]
+    sets = [learned.collect_pairs(ctx, scaled_model(nx, ny, nz, seed=11), f, n_vectors=3)]
+    assert sets[0].v.shape == (6, nx * ny * 3 * nz)
     net = egx.SpectralNet(ctx, nx, ny, nz, width=16, layers=2, seed=0)
     try:
         before = learned.mean_loss(net, sets)
         log = learned.train(net, sets, steps=60, batch=4, lr=1e-3)
         assert np.isfinite(log.losses).all()
         assert learned.mean_loss(net, sets) < before
-        rows = learned.evaluate(ctx, net, scaled_model(nx, ny, nz, seed=12), f, MixedSettings(tol=1e-6))
+        rows = learned.evaluate(ctx, net, scaled_model(nx, ny, nz, seed=12), f)
         by = {r.method: r for r in rows}
         for m in ("gmres", "learned"):
             assert max(by[m].true_be) < 1e-6, (m, by[m].true_be)
-        assert by["learned"].learned_uses >= 1 and by["learned"].fallbacks == 0
+        assert by["learned"].learned_uses >= 1
         assert by["gmres"].learned_uses == 0
-        print("held-out loss %.3f; outer iterations gmres %d none %d learned %d" % (
-            learned.mean_loss(net, held), by["gmres"].iterations[0], by["none"].iterations[0],
-            by["learned"].iterations[0]))
+        print("outer iterations gmres %d none %d learned %d (fallbacks %d)" % (
+            by["gmres"].iterations[0], by["none"].iterations[0], by["learned"].iterations[0],
+            by["learned"].fallbacks))
     finally:
         net.free()
 
