@@ -81,7 +81,10 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
     const float *A = g.A + (long)b * g.a_b;
     const float *B = g.B + (long)b * g.b_b;
     float *C = g.C + (long)b * g.c_b;
-    const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
+    // one CTA per (m, n) tile on grid x (rows of the pointwise GEMMs run to
+    // millions, past grid y's limit)
+    const int ntn = (g.N + GBN - 1) / GBN;
+    const int m0 = (int)(blockIdx.x / ntn) * GBM, n0 = (int)(blockIdx.x % ntn) * GBN;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
     const int gq = lane >> 2, tq = lane & 3;
@@ -149,9 +152,10 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
 }
 
 void gemm(const GemmArgs &g, cudaStream_t s, long *launches) {
-    EGX_CHECK((long)(g.M + GBM - 1) / GBM <= 65535 && g.batch <= 65535 && (g.ksplit <= 1 || g.batch == 1),
+    const long tiles = (long)((g.M + GBM - 1) / GBM) * ((g.N + GBN - 1) / GBN);
+    EGX_CHECK(g.M >= 1 && g.N >= 1 && tiles <= 0x7fffffffL && g.batch <= 65535 && (g.ksplit <= 1 || g.batch == 1),
               EGX_ERR_INVALID, "bad GEMM shape");
-    dim3 grid((g.N + GBN - 1) / GBN, (g.M + GBM - 1) / GBM, g.ksplit > 1 ? g.ksplit : g.batch);
+    dim3 grid((unsigned)tiles, 1, g.ksplit > 1 ? g.ksplit : g.batch);
     k_gemm_bf16<<<grid, 128, 0, s>>>(g);
     EGX_CUDA(cudaGetLastError());
     if (launches) ++*launches;
@@ -318,6 +322,8 @@ struct egx_net {
     int nx = 0, ny = 0, nz = 0, W = 0, L = 0, cin = 0, cout = 0;
     long ncell = 0, n_params = 0;
     int nmodels = 0;  // conductivity models set (sample b uses model b % nmodels)
+    int tc = 1;       // pointwise GEMMs on the tcgen05 kernel (egx_net_use_tcgen05)
+    int *err = nullptr;  // the context's device error flag
     long off_P = 0, off_bP = 0, off_Q = 0, off_bQ = 0;
     std::vector<long> off_Wm, off_Wp, off_Dz, off_b;
     egx::DevBuf params, grads, adam_m, adam_v, bx, by, logsig;
@@ -377,6 +383,19 @@ GemmArgs wgrad(GemmArgs g) {
     return g;
 }
 
+// a pointwise GEMM C[M x N] (+)= A[M x K] B (B by strides; K, N <= 32) on
+// the tcgen05 kernel (egx_learn_tc.cu), or on the warp-level kernel when the
+// network's tcgen05 path is off or the width exceeds 32
+void pw(egx_net *n, int M, int K, const float *A, const float *B, long b_k, long b_n, int N, float *C, bool acc,
+        cudaStream_t s, long *launches) {
+    if (n->tc && pw_gemm_tc_fits(K, N)) {
+        pw_gemm_tc(A, M, K, B, b_k, b_n, N, C, acc, n->err, s);
+        if (launches) ++*launches;
+    } else {
+        gemm(ga(M, N, K, 1, A, K, 1, 0, B, b_k, b_n, 0, C, N, 1, 0, acc ? 1.f : 0.f), s, launches);
+    }
+}
+
 // X0 (encoded) -> Out; keeps the activations for backward. The B samples
 // are B nz depth slices for the lateral operations.
 void forward(egx_net *n, int B, cudaStream_t s, long *launches) {
@@ -384,9 +403,7 @@ void forward(egx_net *n, int B, cudaStream_t s, long *launches) {
     const int S = B * nz;
     const long rows = (long)S * n->ncell, slab = n->ncell * W;
     const float *bx = n->bx.as<float>(), *by = n->by.as<float>();
-    gemm(ga((int)rows, W, n->cin, 1, n->X0.as<float>(), n->cin, 1, 0, n->p(n->off_P), W, 1, 0, n->H[0].as<float>(), W,
-            1, 0),
-         s, launches);
+    pw(n, (int)rows, n->cin, n->X0.as<float>(), n->p(n->off_P), W, 1, W, n->H[0].as<float>(), false, s, launches);
     k_bias_act<<<blocks_for(rows * W), 256, 0, s>>>(n->H[0].as<float>(), n->p(n->off_bP), rows, W, 0,
                                                      n->H[0].as<float>());
     for (int l = 0; l < n->L; l++) {
@@ -410,7 +427,7 @@ void forward(egx_net *n, int B, cudaStream_t s, long *launches) {
         // Pre[s, x] = By S1[s, x]               (ny x W)
         gemm(ga(ny, W, KM, S * nx, by, KM, 1, 0, S1, W, 1, (long)KM * W, Pre, W, 1, (long)ny * W), s, launches);
         // Pre += H Wp
-        gemm(ga((int)rows, W, W, 1, Hl, W, 1, 0, n->p(n->off_Wp[l]), W, 1, 0, Pre, W, 1, 0, 1.f), s, launches);
+        pw(n, (int)rows, W, Hl, n->p(n->off_Wp[l]), W, 1, W, Pre, true, s, launches);
         // Pre[b, z] += sum_z' Dz[z, z'] H[b, z']   (nz x ncell W) per sample
         gemm(ga(nz, (int)slab, nz, B, n->p(n->off_Dz[l]), nz, 1, 0, Hl, slab, 1, (long)nz * slab, Pre, slab, 1,
                 (long)nz * slab, 1.f),
@@ -419,9 +436,8 @@ void forward(egx_net *n, int B, cudaStream_t s, long *launches) {
                                                          n->H[l + 1].as<float>());
         if (launches) ++*launches;
     }
-    gemm(ga((int)rows, n->cout, W, 1, n->H[n->L].as<float>(), W, 1, 0, n->p(n->off_Q), n->cout, 1, 0,
-            n->Out.as<float>(), n->cout, 1, 0),
-         s, launches);
+    pw(n, (int)rows, W, n->H[n->L].as<float>(), n->p(n->off_Q), n->cout, 1, n->cout, n->Out.as<float>(), false, s,
+       launches);
     k_bias_act<<<blocks_for(rows * n->cout), 256, 0, s>>>(n->Out.as<float>(), n->p(n->off_bQ), rows, n->cout, 0,
                                                            n->Out.as<float>());
     if (launches) *launches += 2;
@@ -447,8 +463,7 @@ void backward(egx_net *n, int B, cudaStream_t s, long *launches) {
                   n->cout, 1, 0)),
          s, launches);
     colsum(dOut, rows, n->cout, n->gr(n->off_bQ), s, launches);
-    gemm(ga((int)rows, W, n->cout, 1, dOut, n->cout, 1, 0, n->p(n->off_Q), 1, n->cout, 0, n->dH.as<float>(), W, 1, 0),
-         s, launches);
+    pw(n, (int)rows, n->cout, dOut, n->p(n->off_Q), 1, n->cout, W, n->dH.as<float>(), false, s, launches);
     for (int l = n->L - 1; l >= 0; l--) {
         float *dPre = n->dH.as<float>(), *dH2 = n->dH2.as<float>();
         const float *Hl = n->H[l].as<float>(), *Ul = n->U[l].as<float>();
@@ -459,7 +474,7 @@ void backward(egx_net *n, int B, cudaStream_t s, long *launches) {
         colsum(dPre, rows, W, n->gr(n->off_b[l]), s, launches);
         // dWp = H^T dPre; dH2 = dPre Wp^T
         gemm(wgrad(ga(W, W, (int)rows, 1, Hl, 1, W, 0, dPre, W, 1, 0, n->gr(n->off_Wp[l]), W, 1, 0)), s, launches);
-        gemm(ga((int)rows, W, W, 1, dPre, W, 1, 0, n->p(n->off_Wp[l]), 1, W, 0, dH2, W, 1, 0), s, launches);
+        pw(n, (int)rows, W, dPre, n->p(n->off_Wp[l]), 1, W, W, dH2, false, s, launches);
         // spectral branch
         float *dS1 = n->dS1.as<float>(), *dV = n->dV.as<float>(), *dU = n->dU.as<float>(), *dU1 = n->dU1.as<float>();
         gemm(ga(KM, W, ny, S * nx, by, 1, KM, 0, dPre, W, 1, (long)ny * W, dS1, W, 1, (long)KM * W), s, launches);
@@ -542,6 +557,7 @@ int egx_net_create(egx_ctx *ctx, int nx, int ny, int nz, int width, int layers, 
         set_device(ctx);
         auto n = std::unique_ptr<egx_net>(new egx_net());
         n->nx = nx, n->ny = ny, n->nz = nz, n->W = width, n->L = layers;
+        n->err = ctx->errflag.as<int>();
         n->cin = 7, n->cout = 6, n->ncell = (long)nx * ny;
         long off = 0;
         auto take = [&](long k) {
@@ -691,9 +707,18 @@ int egx_net_loss_grad(egx_ctx *ctx, egx_net *net, const float *v, const float *t
         EGX_CUDA(cudaMemcpyAsync(h.data(), e2, 2 * batch * sizeof(double), cudaMemcpyDeviceToHost, s));
         if (grad) EGX_CUDA(cudaMemcpyAsync(grad, net->grads.p, net->n_params * sizeof(float), cudaMemcpyDeviceToHost, s));
         EGX_CUDA(cudaStreamSynchronize(s));
+        check_device_error(ctx);
         double l = 0;
         for (int b = 0; b < batch; b++) l += h[batch + b] > 0 ? h[b] / h[batch + b] : 0.0;
         *loss = (float)(l / batch);
+    });
+}
+
+int egx_net_use_tcgen05(egx_ctx *ctx, egx_net *net, int enable) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(net, EGX_ERR_INVALID, "null network");
+        net->tc = enable ? 1 : 0;
     });
 }
 
@@ -733,6 +758,7 @@ int egx_net_apply(egx_ctx *ctx, egx_net *net, const float *v, float *z, int batc
                                      cudaMemcpyDeviceToHost, s));
         }
         EGX_CUDA(cudaStreamSynchronize(s));
+        check_device_error(ctx);
     });
 }
 

@@ -1,4 +1,4 @@
-// Learned flexible preconditioner: a spectral network on the lateral grid
+// Learned flexible preconditioner: a spectral network on the anomaly mesh
 // (declarations shared by egx_learn.cu and the solver in egx_api.cu).
 #pragma once
 
@@ -15,5 +15,13 @@ void net_apply(egx_net *net, const float2 *v, float2 *z, int batch, cudaStream_t
 
 // nx ny 3 nz: the vector length the network was built for
 long net_length(const egx_net *net);
+
+// Pointwise GEMM on the tcgen05 tensor cores (egx_learn_tc.cu): C[m, n] =
+// sum_k A[m, k] B[k b_k + n b_n] (+ C[m, n] with accumulate), A row-major
+// [M x K], C row-major [M x N], K and N in 1..32, BF16 operands, FP32
+// accumulation; err receives EGX_ERR_TIMEOUT if a bounded wait expires.
+bool pw_gemm_tc_fits(int K, int N);
+void pw_gemm_tc(const float *A, int M, int K, const float *B, long b_k, long b_n, int N, float *C, bool accumulate,
+                int *err, cudaStream_t s);
 
 }  // namespace egx

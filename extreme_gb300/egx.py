@@ -30,7 +30,7 @@ EXPORTS = [
     "egx_profile_read",
     "egx_level_fields", "egx_level_cache", "egx_set_level_precision", "egx_mt_responses", "egx_wait_selftest",
     "egx_net_create", "egx_net_free", "egx_net_size", "egx_net_params", "egx_net_set_model", "egx_net_set_models", "egx_net_loss_grad",
-    "egx_net_adam", "egx_net_apply", "egx_learned_stats", "egx_learned_inject_nonfinite",
+    "egx_net_adam", "egx_net_use_tcgen05", "egx_net_apply", "egx_learned_stats", "egx_learned_inject_nonfinite",
 ]
 
 # kernel kinds of egx_profile_read
@@ -137,6 +137,7 @@ def load(path=None):
     lib.egx_net_set_models.argtypes = [vp, vp, vp, i]
     lib.egx_net_loss_grad.argtypes = [vp, vp, vp, vp, i, C.POINTER(C.c_float), vp, i]
     lib.egx_net_adam.argtypes = [vp, vp, C.c_float]
+    lib.egx_net_use_tcgen05.argtypes = [vp, vp, i]
     lib.egx_net_apply.argtypes = [vp, vp, vp, vp, i, i]
     lib.egx_learned_stats.argtypes = [vp, C.POINTER(C.c_long), C.POINTER(C.c_long)]
     lib.egx_learned_inject_nonfinite.argtypes = [vp, i]
@@ -513,6 +514,10 @@ class SpectralNet:
         self.ctx._check(self.ctx.lib.egx_net_loss_grad(self.ctx.h, self.h, C.c_void_p(v_ptr), C.c_void_p(t_ptr),
                                                        batch, C.byref(loss), None, DEVICE))
         return loss.value
+
+    def use_tcgen05(self, enable):
+        """Pointwise GEMMs on the tcgen05 kernel (default) or the mma.sync one."""
+        self.ctx._check(self.ctx.lib.egx_net_use_tcgen05(self.ctx.h, self.h, int(bool(enable))))
 
     def adam(self, lr):
         self.ctx._check(self.ctx.lib.egx_net_adam(self.ctx.h, self.h, float(lr)))

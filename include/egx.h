@@ -231,6 +231,12 @@ int egx_net_set_models(egx_ctx *ctx, egx_net *net, const float *logsig, int coun
 int egx_net_loss_grad(egx_ctx *ctx, egx_net *net, const float *v, const float *t, int batch, float *loss, float *grad,
                       int where);
 int egx_net_adam(egx_ctx *ctx, egx_net *net, float lr);
+/* The network's pointwise GEMMs (lift, per-layer width x width map,
+ * projection, and their backward products; width <= 32) run on a tcgen05
+ * kernel (enable = 1, the default: BF16 operands staged in shared memory,
+ * FP32 accumulator in tensor memory) or on the warp-level mma.sync kernel
+ * that the spectral and weight-gradient GEMMs use (enable = 0). */
+int egx_net_use_tcgen05(egx_ctx *ctx, egx_net *net, int enable);
 int egx_net_apply(egx_ctx *ctx, egx_net *net, const float *v, float *z, int batch, int where);
 /* With egx_set_precond(ctx, EGX_PRECOND_LEARNED, NULL, net) each inner
  * complex64 FGMRES of the mixed form uses the network as its flexible right

@@ -145,7 +145,15 @@ def test_mixed_solve_with_learned_preconditioner(ctx):
     preconditioner: whatever the network's quality, the solve reaches the
     1e-6 target (the GMRES preconditioner takes over for an inner solve the
     network does not finish in four cycles), and the reference's method is
-    unchanged beside it."""
+    unchanged beside it.
+
+    No gain is asserted, because none was measured: trained on 2,000
+    seeded 128x128x32 solves, the network predicts 32 % of the held-out
+    correction energy (held-out loss 0.68), too little to converge within
+    its four-cycle budget, so the held-out solves fall back and cost the
+    budget on top of the GMRES-preconditioned applies (247 against 123 at
+    0.01 Hz). What is asserted is that bound: the learned form never costs
+    more than the budget plus the reference method."""
     from extreme_gb300 import egx, learned
     from extreme_gb300.model import scaled_model
     nx, ny, nz = 24, 24, 4
@@ -164,6 +172,11 @@ def test_mixed_solve_with_learned_preconditioner(ctx):
             assert max(by[m].true_be) < 1e-6, (m, by[m].true_be)
         assert by["learned"].learned_uses >= 1
         assert by["gmres"].learned_uses == 0
+        # four FGMRES(30) cycles of the network (one residual apply each),
+        # then the GMRES-preconditioned solve
+        budget = 4 * (30 + 1)
+        assert by["learned"].applies[0] <= by["gmres"].applies[0] + budget + 2, (by["learned"].applies,
+                                                                                   by["gmres"].applies)
         print("outer iterations gmres %d none %d learned %d (fallbacks %d)" % (
             by["gmres"].iterations[0], by["none"].iterations[0], by["learned"].iterations[0],
             by["learned"].fallbacks))
@@ -185,4 +198,36 @@ def test_learned_net_must_match_the_grid(ctx):
             solver.solve(m, 1.0)
     finally:
         ctx.set_learned(None)
+        net.free()
+
+
+def test_tcgen05_pointwise_gemms_match_the_warp_level_kernel(ctx):
+    """The network's pointwise GEMMs on the tcgen05 kernel (BF16 operands in
+    shared memory, FP32 accumulator in tensor memory; the default) and on the
+    warp-level mma.sync kernel round the same operands to BF16: loss, every
+    gradient block and the apply agree to FP32 summation-order differences,
+    and both stay within the BF16 bound of the FP64 oracle. The mesh has
+    rows that do not fill the last 128-row tile."""
+    nx, ny, nz, W, L, B = 18, 14, 5, 32, 3, 3
+    net, flat, lay = _net(ctx, nx, ny, nz, W, L, seed=9)
+    try:
+        v, t, logsig = _inputs(nx, ny, nz, B, seed=9)
+        net.set_model(logsig)
+        out = {}
+        for tc in (True, False):
+            net.use_tcgen05(tc)
+            loss, g = net.loss_grad(v, t, want_grad=True)
+            out[tc] = (loss, g, net.apply(v))
+        net.use_tcgen05(True)
+        (l1, g1, z1), (l0, g0, z0) = out[True], out[False]
+        assert abs(l1 - l0) <= 1e-4 * l0, (l1, l0)
+        for name, (off, shape) in lay.items():
+            k = int(np.prod(shape))
+            a, b = g1[off:off + k], g0[off:off + k]
+            assert np.linalg.norm(a - b) <= 1e-3 * max(np.linalg.norm(b), 1e-30), name
+        assert np.linalg.norm(z1 - z0) <= 1e-4 * np.linalg.norm(z0 - v)
+        ref_loss, _ = sn.loss_grad(flat, v.astype(np.complex128), t.astype(np.complex128),
+                                   logsig.astype(np.float64), nx, ny, nz, W, L)
+        assert abs(l1 - ref_loss) <= LOSS_TOL * ref_loss
+    finally:
         net.free()
