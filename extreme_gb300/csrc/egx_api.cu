@@ -626,9 +626,12 @@ int egx_tune_apply(egx_ctx *ctx, int nrhs, int reps, double *ms_out) {
         EGX_CUDA(cudaEventCreate(&b));
         double best = 1e300;
         int bt = 0, bv = 0;
-        // the packed layout has three contraction kernels to choose from; the
-        // sub-block layout (nz in 16, 32, 48) one
-        const int nvar = sb_layout(ctx->nz) ? 1 : 3;
+        // three contraction kernels to choose from in either Green layout:
+        // packed (tensor-core, TMA-staged CUDA-core, generic) or sub-block
+        // for nz in 16, 32, 48 (built-in, k_contract_sb3 with the reduction
+        // on the first MT warps, k_contract_sb3 with it spread over the
+        // warps that have the fewest column tiles)
+        const int nvar = 3;
         for (int tile = 0; tile < 3; tile++)
             for (int var = 0; var < nvar; var++) {
                 ctx->fft_tile = tile;

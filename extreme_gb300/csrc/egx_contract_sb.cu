@@ -449,7 +449,7 @@ struct Sb3 {
     __host__ __device__ static constexpr int kt0(int kg) { return kg * KT / KG; }
 };
 
-template <int NZ>
+template <int NZ, bool BAL>
 __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
     k_contract_sb3(float2 *buf, const float2 *__restrict__ G, const int nx, const int ny, const int B, const int rhs0,
                    int *err) {
@@ -461,6 +461,20 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
     const int g = lane >> 2, t = lane & 3;
     const int mg = warp % P::MG, kg = warp / P::MG;
     const int ktb = P::kt0(kg), kcnt = P::kt0(kg + 1) - ktb;
+    // warps of the column groups with the fewest column tiles, numbered
+    // 0 .. nlight-1 (light = -1 for the others)
+    int light = -1, nlight = 0;
+    {
+        int mincnt = P::KT;
+        for (int k = 0; k < P::KG; k++) mincnt = min(mincnt, P::kt0(k + 1) - P::kt0(k));
+        for (int w = 0; w < P::MG * P::KG; w++) {
+            const int wk = w / P::MG;
+            if (P::kt0(wk + 1) - P::kt0(wk) == mincnt) {
+                if (w == warp) light = nlight;
+                nlight++;
+            }
+        }
+    }
     const uint32_t sG = saddr(smem), sX = sG + P::OFF_X;
     const uint32_t bar0 = saddr(&bars[0]);
     const long Q = (long)(nx + 1) * (ny + 1);
@@ -615,11 +629,17 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(q + 2L * gridDim.x, stage);
         }
-        // warp w < MT adds the column groups' partials of row tile w and stores
-        if (warp < P::MT) {
-            const int mt = warp;
+        // reduction units: with BAL, the 2 MT half row tiles (rows g or g + 8)
+        // over the warps of the column groups with the fewest column tiles;
+        // else row tile w by warp w < MT
+        const int ubeg = BAL ? (light >= 0 ? light : 2 * P::MT) : (warp < P::MT ? warp : P::MT);
+        const int uend = BAL ? 2 * P::MT : (warp < P::MT ? warp + 1 : P::MT);
+        const int ustep = BAL ? nlight : 1;
+        for (int u = ubeg; u < uend; u += ustep) {
+            const int mt = BAL ? u >> 1 : u;
 #pragma unroll
             for (int c = 0; c < 4; c++) {
+                if (BAL && (c >> 1) != (u & 1)) continue;
                 float yr = 0.f, yi = 0.f;
 #pragma unroll
                 for (int k = 0; k < P::KG; k++) {
@@ -643,13 +663,13 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
     }
 }
 
-template <int NZ>
+template <int NZ, bool BAL>
 void launch_sb3(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err, cudaStream_t s, int nsm) {
     using P = Sb3<NZ>;
-    raise_smem_limit((const void *)k_contract_sb3<NZ>, P::SMEM);
+    raise_smem_limit((const void *)k_contract_sb3<NZ, BAL>, P::SMEM);
     const long Q = (long)(d.nx + 1) * (d.ny + 1);
     const unsigned grid = (unsigned)std::min<long>(Q, nsm);
-    k_contract_sb3<NZ><<<grid, P::THREADS, P::SMEM, s>>>(buf, G, d.nx, d.ny, d.B, rhs0, err);
+    k_contract_sb3<NZ, BAL><<<grid, P::THREADS, P::SMEM, s>>>(buf, G, d.nx, d.ny, d.B, rhs0, err);
     EGX_CUDA(cudaGetLastError());
 }
 
@@ -665,9 +685,16 @@ void launch_sb(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err
 
 template <int NZ>
 void launch_nz(float2 *buf, const float2 *G, const OpDims &d, int *err, cudaStream_t s, int nsm, long *launches) {
+    // contract_variant: 1 / 2 k_contract_sb3 without / with the balanced
+    // reduction, 0 the built-in choice: balanced (2.265 against 2.294 ms per
+    // two-source apply at 256x256x48, bitwise the same sums)
+    const int v = d.contract_variant;
     for (int r0 = 0; r0 < d.nrhs;) {
         if (d.nrhs - r0 >= 2) {
-            launch_sb3<NZ>(buf, G, d, r0, err, s, nsm);
+            if (v != 1)
+                launch_sb3<NZ, true>(buf, G, d, r0, err, s, nsm);
+            else
+                launch_sb3<NZ, false>(buf, G, d, r0, err, s, nsm);
             r0 += 2;
         } else {
             launch_sb<NZ, 1>(buf, G, d, r0, err, s, nsm);

@@ -137,8 +137,8 @@ __global__ void __launch_bounds__(reg_threads<N, T, BT>(), reg_min_blocks<N, T, 
     k_fwd_y_r(const C<T> *__restrict__ x, const OperatorData<T> op, C<T> *__restrict__ buf, const OpDims d,
               const C<T> *__restrict__ tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int i = blockIdx.x;
-    const int b = blockIdx.y * BT + (int)(threadIdx.x % BT);
+    const int i = blockIdx.y;
+    const int b = blockIdx.x * BT + (int)(threadIdx.x % BT);
     const bool bok = b < d.B;
     const int per = 3 * d.nz;
     const int rhs = bok ? b / per : 0, rem = b - rhs * per, k = rem % d.nz;
@@ -160,9 +160,9 @@ __global__ void __launch_bounds__(reg_threads<N, T, BT>())
     k_lines_r(C<T> *buf, long lstride, long estride, int B, int nload, int nstore, const C<T> *__restrict__ tw,
               int sign) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int b = blockIdx.y * BT + (int)(threadIdx.x % BT);
+    const int b = blockIdx.x * BT + (int)(threadIdx.x % BT);
     const bool bok = b < B;
-    C<T> *line = buf + (long)blockIdx.x * lstride + b;
+    C<T> *line = buf + (long)blockIdx.y * lstride + b;
     auto load = [&](int e) -> C<T> { return (bok && e < nload) ? line[e * estride] : mk<T>(0, 0); };
     auto store = [&](int e, C<T> v) {
         if (bok && e < nstore) line[e * estride] = v;
@@ -175,8 +175,8 @@ __global__ void __launch_bounds__(reg_threads<N, T, BT>(), reg_min_blocks<N, T, 
     k_bwd_y_r(const C<T> *__restrict__ buf, const C<T> *__restrict__ x, const OperatorData<T> op,
               C<T> *__restrict__ y, const OpDims d, const C<T> *__restrict__ tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int i = blockIdx.x;
-    const int b = blockIdx.y * BT + (int)(threadIdx.x % BT);
+    const int i = blockIdx.y;
+    const int b = blockIdx.x * BT + (int)(threadIdx.x % BT);
     const bool bok = b < d.B;
     const int per = 3 * d.nz;
     const int rhs = bok ? b / per : 0, rem = b - rhs * per, k = rem % d.nz;
@@ -232,7 +232,10 @@ static void launch_reg(int which, cudaStream_t s, int nlines, const C<T> *x, con
                        const C<T> *tw, int sign) {
     constexpr size_t sm = reg_smem<N, T, BT>();
     constexpr int thr = reg_threads<N, T, BT>();
-    const dim3 grid(nlines, (B + BT - 1) / BT);
+    // column tiles on x: the CTAs in flight together cover whole rows of a
+    // line (every column of an (x, y) point's 3 nz values, per source),
+    // rather than one tile of many lines, so DRAM sees long runs
+    const dim3 grid((B + BT - 1) / BT, nlines);
     if (which == 0) {
         reg_attr<T, N, BT>((const void *)k_fwd_y_r<T, N, BT>);
         k_fwd_y_r<T, N, BT><<<grid, thr, sm, s>>>(x, *op, buf, *d, tw);

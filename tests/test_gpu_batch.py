@@ -74,11 +74,12 @@ def test_graph_captured_inner_cycle_matches_launches(egx_ctx):
 
 def test_apply_tuner_variants_agree(egx_ctx):
     """Every kernel variant the apply tuner times gives the same apply (to
-    complex64 rounding), on the packed Green layout (nz = 7, three
-    contraction kernels) and the sub-block layout (nz = 16)."""
+    complex64 rounding), on the packed Green layout (nz = 7: tensor-core,
+    TMA-staged and generic contraction kernels) and the sub-block layout
+    (nz = 16, 48: k_contract_sb3 with either reduction layout)."""
     from extreme_gb300.forward import model_zeta
     from extreme_gb300.model import freq_to_omega
-    for nz in (7, 16):
+    for nz in (7, 16, 48):
         m = random_model(16, 12, nz, seed=6)
         omega = freq_to_omega(1.0)
         g = egx_ctx.green_build(m, omega, 10, egx.PREC_MIXED)
@@ -86,7 +87,7 @@ def test_apply_tuner_variants_agree(egx_ctx):
             zeta, zeta0 = model_zeta(m, omega)
             egx_ctx.op_prepare(g, zeta, zeta0, m.layer_thickness, egx.OP_A)
             tile, var, table = egx_ctx.tune_apply(nrhs=2, reps=2)
-            assert (tile, var) in table and len(table) == (3 if nz == 16 else 9)
+            assert (tile, var) in table and len(table) == 9
             n = m.nx * m.ny * 3 * m.nz
             rng = np.random.default_rng(7)
             x = (rng.standard_normal(2 * n) + 1j * rng.standard_normal(2 * n)).astype(np.complex64)
