@@ -444,7 +444,7 @@ def run_ours(args, rank, world, local):
     peak, peak_src = load_peaks()
     achieved = alg_bytes / (kms / kc / 1e3) / 1e9 if kc else None
     if m.nz in (16, 32, 48):
-        kname = "k_contract_sb3" if rhs == 2 else "k_contract_sb"
+        kname = "k_contract_sh" if rhs == 2 else "k_contract_sb"
     else:  # packed layout: the tensor-core kernel takes one source, the TMA kernel two
         kname = "k_contract_c64" if rhs == 2 else "k_contract_mma"
     roofline = {"kernel": kname, "bound": "hbm", "rhs_per_launch": rhs,

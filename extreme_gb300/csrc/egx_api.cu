@@ -176,9 +176,10 @@ GmresResult run_fgmres(egx_ctx *ctx, const C<T> *b, C<T> *x, int m_out, int m_in
             (*outer)->precond = [ctx, in, vb, tol, nrhs](const C<T> *src, C<T> *dst) {
                 C<T> *pin = ctx->pc_in.as<C<T>>(), *pout = ctx->pc_out.as<C<T>>();
                 char key[512];
-                snprintf(key, sizeof key, "%p/%p/%p/%p/%p/%p/%p/%p/%p/%p/%p/%d/%d/%.17g/%zu", (void *)in, ctx->g,
+                snprintf(key, sizeof key, "%p/%p/%p/%p/%p/%p/%p/%p/%p/%p/%p/%d/%d/%.17g/%zu/%d/%d", (void *)in, ctx->g,
                          ctx->g->g32.p, ctx->g->g64.p, ctx->r32.p, ctx->r64.p, ctx->buf32.p, ctx->buf64.p,
-                         ctx->tw0_32.p, (void *)pin, (void *)pout, ctx->type, nrhs, tol, vb);
+                         ctx->tw0_32.p, (void *)pin, (void *)pout, ctx->type, nrhs, tol, vb, ctx->fft_tile,
+                         ctx->contract_variant);
                 EGX_CUDA(cudaMemcpyAsync(pin, src, vb, cudaMemcpyDeviceToDevice, ctx->stream));
                 if (ctx->pc_key != key || !ctx->pc_exec) {
                     if (ctx->pc_exec) EGX_CUDA(cudaGraphExecDestroy(ctx->pc_exec));

@@ -1,7 +1,7 @@
 // Block contraction of the CIE operator in complex64 on the tensor cores
 // (ConvolutionOperator.ApplyGreenTensorAlongZ, ConvolutionOperator.cs:274-327)
 // for nz in {16, 32, 48}, one or two right-hand sides per pass, reading the
-// complex64 Green copy in a 4x4 sub-block layout.
+// mixed form's Green copy in a 4x4 sub-block layout.
 //
 // Sub-block layout of one stored spectral point (nb = nz/4):
 //   xx | xy | yy | zz : the nb(nb+1)/2 upper-triangle 4x4 sub-blocks (I <= J)
@@ -12,32 +12,40 @@
 // Every fragment load of a half-warp (4 rows x 4 columns of G, either
 // orientation) then falls in one 128-byte sub-block: conflict-free.
 //
-// Algebra as in the other contraction kernels: the four spectral points
-// sharing a stored block are right-hand sides of one (3nz x 3nz) complex
-// matrix after D_p sign flips, the complex product is embedded in real
-// arithmetic [Yr | Yi] = Gr [Xr | Xi] + Gi [-Xi | Xr], and each TF32 operand
-// is split into a rounded high part and a remainder (three products per
-// pair: hi.hi + hi.lo + lo.hi), which keeps complex64 accuracy.
+// Each 8-byte entry holds the Green value scaled by one power of two for
+// the whole tensor and split into FP16 high parts and remainders of Re and
+// Im (split_entry: 22 significant bits, the precision of a TF32 split); the
+// trailing entry of the copy holds the largest magnitude and 1/scale.
+//
+// Algebra: the four spectral points sharing a stored block are right-hand
+// sides of one (3nz x 3nz) complex matrix after D_p sign flips; each product
+// of split operands takes three MMAs (hi.hi + hi.lo + lo.hi), which keeps
+// complex64 accuracy.
 //
 // Work split per CTA (one per SM, loop over stored points): 12 warps as
 // 3 row groups x 4 column groups; each warp owns 1/3 of the 16-row tiles and
-// 1/4 of the 8-column tiles, keeps the offsets of its A fragments in
-// registers (built once), and accumulates one partial product per row tile.
+// a quarter of the column tiles, keeps the offsets of its A fragments in
+// registers (built once), and accumulates partial products per row tile.
 // The -A^T blocks (z rows, x|y columns) are exactly the tiles of row group 2
 // and the x|y column tiles, so their sign goes onto those warps' B values.
-// The column groups' partial sums meet in shared memory, where warp w < MT
-// adds those of row tile w and stores.
+// The column groups' partial sums meet in shared memory and are added and
+// stored by the warps with the fewest column tiles.
 //
-// Two kernels: k_contract_sb<NZ, 1> for one right-hand side, and
-// k_contract_sb3<NZ> for two (the stacked solve of both polarisations),
-// which uses three real products per complex product (below).
+// Three kernels: k_contract_sh<NZ> for two right-hand sides (the stacked
+// solve of both polarisations: FP16 m16n8k16, A fragments straight from the
+// split entries), k_contract_sb3<NZ> for two on the TF32 m16n8k8 path (the
+// entries recombined to complex64 first; the tuner's alternative), and
+// k_contract_sb<NZ, 1> for one (TF32, recombined entries).
 //
 // Per stored point: one TMA bulk copy of the block and one per present
 // right-hand-side segment into one of two stages, issued two points ahead
 // and completing on the stage's mbarrier (waits bounded to 2 s; on expiry
 // EGX_ERR_TIMEOUT is recorded in *err and the kernel returns).
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <cstdint>
+#include <cstring>
 
 #include "egx_krylov.cuh"
 #include "egx_operator.cuh"
@@ -90,6 +98,38 @@ __device__ __forceinline__ void split_rn(float a, uint32_t &hi, uint32_t &lo) {
     lo = tf32_hi(__float_as_uint(a - __uint_as_float(hi)));
 }
 
+// 2^(top - e) with 2^(e-1) <= m < 2^e for a normal m > 0, the exponent
+// read from the bit pattern; 1 for zero, subnormal or non-finite m
+__host__ __device__ inline float pow2_scale(float m, int top) {
+    uint32_t u;
+    memcpy(&u, &m, 4);
+    const int ef = (int)((u >> 23) & 0xffu);
+    if (ef == 0 || ef == 255) return 1.f;
+    int k = top - (ef - 126);
+    k = k > 127 ? 127 : (k < -126 ? -126 : k);
+    const uint32_t r = (uint32_t)(127 + k) << 23;
+    float f;
+    memcpy(&f, &r, 4);
+    return f;
+}
+
+// One entry of the split Green copy: the scaled Re and Im as FP16 high
+// parts (rounded to 11 significant bits) and FP16 remainders,
+// x = Re hi | Im hi << 16, y = Re lo | Im lo << 16; hi + lo keeps 22 bits.
+__device__ __forceinline__ uint2 split_entry(float re, float im) {
+    const float rh = __uint_as_float(tf32_hi(__float_as_uint(re)));
+    const float ih = __uint_as_float(tf32_hi(__float_as_uint(im)));
+    const __half2 h = __floats2half2_rn(rh, ih), l = __floats2half2_rn(re - rh, im - ih);
+    return make_uint2(*reinterpret_cast<const uint32_t *>(&h), *reinterpret_cast<const uint32_t *>(&l));
+}
+
+// the complex64 value of a split entry (inv undoes the copy's scale)
+__device__ __forceinline__ float2 unsplit_entry(uint2 u, float inv) {
+    const float2 h = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
+    const float2 l = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
+    return make_float2((h.x + l.x) * inv, (h.y + l.y) * inv);
+}
+
 __device__ __forceinline__ void mma_tf32(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
     asm(
         "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -125,12 +165,26 @@ __host__ __device__ inline int sb_index(int nz, int row, int col) {
     return 4 * S + ci * A + ((j >> 2) * nb + (i >> 2)) * 16 + (j & 3) * 4 + (i & 3);
 }
 
-// complex128 packed quadrant (GreenDims layout) -> complex64 sub-block layout
-__global__ void k_repack_sb(const double2 *__restrict__ g64, float2 *__restrict__ g32, long Q, int nz) {
+// complex128 packed quadrant (GreenDims layout) -> the split sub-block copy.
+// Two passes over the same index map: the first (WRITE false) takes the
+// largest |Re|, |Im| into tail[0] (as its bit pattern, which orders like the
+// value for non-negative floats; zeroed by the caller); the second scales by
+// s = 2^(14 - e), 2^e above that largest magnitude (so |Re| + |Im| < 2^15
+// fits FP16), writes the split entries and 1/s into tail[1]. tail is the
+// copy's trailing entry, g32[Q BS].
+template <bool WRITE>
+__global__ void k_repack_sb(const double2 *__restrict__ g64, uint2 *__restrict__ g32, long Q, int nz) {
     const int S = sb_sym(nz), A = sb_asy(nz), BS = 4 * S + 2 * A, nb = nz / 4;
     // packed layout (GreenDims): S0 per symmetric block, rows of xz/yz padded to nz + 1
     const int S0 = nz * (nz + 1) / 2, lda = nz + 1, A0 = nz * lda, BS0 = 4 * S0 + 2 * A0;
     const long total = Q * BS;
+    uint32_t *tail = reinterpret_cast<uint32_t *>(g32 + total);
+    float scale = 1.f;
+    if (WRITE) {
+        scale = pow2_scale(__uint_as_float(tail[0]), 14);
+        if (blockIdx.x == 0 && threadIdx.x == 0) tail[1] = __float_as_uint(1.f / scale);
+    }
+    float vmax = 0.f;
     for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
         const long q = idx / BS;
         const int d = (int)(idx - q * BS);
@@ -149,7 +203,14 @@ __global__ void k_repack_sb(const double2 *__restrict__ g64, float2 *__restrict_
             src = 4 * S0 + co * A0 + (4 * I + (e >> 2)) * lda + 4 * J + (e & 3);
         }
         const double2 v = g64[q * BS0 + src];
-        g32[idx] = make_float2((float)v.x, (float)v.y);
+        if (WRITE)
+            g32[idx] = split_entry((float)(v.x * scale), (float)(v.y * scale));
+        else
+            vmax = fmaxf(vmax, fmaxf(fabsf((float)v.x), fabsf((float)v.y)));
+    }
+    if (!WRITE) {
+        const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(vmax));
+        if ((threadIdx.x & 31) == 0 && m) atomicMax(tail, m);
     }
 }
 
@@ -196,6 +257,8 @@ __global__ void __launch_bounds__(Sb<NZ, NRHS>::THREADS, 1)
     const uint32_t bar0 = saddr(&bars[0]);
     const long Q = (long)(nx + 1) * (ny + 1);
     const int n1 = 2 * ny;
+    // 1 / the split copy's scale, in its trailing entry
+    const float ginv = __uint_as_float(reinterpret_cast<const uint2 *>(G)[Q * P::BS].y);
 
     // offsets (complex units) of this lane's A-fragment entries: pair
     // (row tile mg*MPW + im, column tile ktb + ik), entries e = 0..3, two
@@ -306,7 +369,7 @@ __global__ void __launch_bounds__(Sb<NZ, NRHS>::THREADS, 1)
         // plain shared-memory reads: the compiler may schedule them freely
         // between the barriers that order them against the stage's TMA and
         // the B-fragment pass
-        const float2 *Gq = reinterpret_cast<const float2 *>(smem + stage * P::G_BYTES);
+        const uint2 *Gq = reinterpret_cast<const uint2 *>(smem + stage * P::G_BYTES);
         const uint4 *BFq = reinterpret_cast<const uint4 *>(smem + P::OFF_BF) + lane;
 #pragma unroll
         for (int ik = 0; ik < KMAX; ik++) {
@@ -336,7 +399,7 @@ __global__ void __launch_bounds__(Sb<NZ, NRHS>::THREADS, 1)
                 const uint32_t off[4] = {t0 & 0xffffu, t0 >> 16, t1 & 0xffffu, t1 >> 16};
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
-                    const float2 gv = Gq[off[e]];
+                    const float2 gv = unsplit_entry(Gq[off[e]], ginv);
                     split(gv.x, af[im][0][e], af[im][1][e]);
                     split(gv.y, af[im][2][e], af[im][3][e]);
                 }
@@ -479,6 +542,8 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
     const uint32_t bar0 = saddr(&bars[0]);
     const long Q = (long)(nx + 1) * (ny + 1);
     const int n1 = 2 * ny;
+    // 1 / the split copy's scale, in its trailing entry
+    const float ginv = __uint_as_float(reinterpret_cast<const uint2 *>(G)[Q * P::BS].y);
     // this lane's B column: point v, source rb
     const int bv = g & 3, brs = g >> 2, bmx = bv >> 1, bmy = bv & 1;
 
@@ -558,7 +623,7 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
             for (int j = 0; j < 3; j++)
 #pragma unroll
                 for (int c = 0; c < 4; c++) acc[im][j][c] = 0.f;
-        const float2 *Gq = reinterpret_cast<const float2 *>(smem + stage * P::G_BYTES);
+        const uint2 *Gq = reinterpret_cast<const uint2 *>(smem + stage * P::G_BYTES);
 #pragma unroll
         for (int ik = 0; ik < KMAX; ik++) {
             if (ik >= kcnt) break;
@@ -593,7 +658,7 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
                 const uint32_t off[4] = {t0 & 0xffffu, t0 >> 16, t1 & 0xffffu, t1 >> 16};
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
-                    const float2 gv = Gq[off[e]];
+                    const float2 gv = unsplit_entry(Gq[off[e]], ginv);
                     split(gv.x, af[0][e], af[1][e]);
                     split(gv.y, af[2][e], af[3][e]);
                     split(gv.x + gv.y, af[4][e], af[5][e]);
@@ -663,6 +728,321 @@ __global__ void __launch_bounds__(Sb3<NZ>::THREADS, 1)
     }
 }
 
+// Two right-hand sides on the FP16 tensor-core path. The split copy holds
+// every Green entry as FP16 high parts and remainders of its scaled Re and
+// Im (split_entry), so the A fragments of mma.sync m16n8k16 come straight
+// from shared memory, two entries and four byte permutes per register
+// quartet, with no conversion. The right-hand sides are scaled per column
+// by a power of two (2^(13 - e) over the rows this warp multiplies; the four
+// lanes of a column agree by shuffle) and split the same way in registers.
+// Four real products per complex product, three FP16 passes each
+// (hi.hi + hi.lo + lo.hi, 22 bits per operand as the TF32 split):
+//   T1 = Gr Xr, T2 = Gi Xi, T3 = Gr Xi, T4 = Gi Xr, Yr = T1 - T2, Yi = T3 + T4,
+// 12 MMAs of K = 16 per (row tile, column tile) pair where the TF32 form
+// takes 18 of K = 8 for the same K. Each warp divides its partial sums by
+// its scales before they meet.
+//
+// Work split as k_contract_sb3 (12 warps, 3 row groups x 4 column groups,
+// column tiles of 16, two TMA stages, two block barriers per point, the
+// reduction on the warps with the fewest column tiles).
+template <int NZ>
+struct Sh {
+    static constexpr int R = 3 * NZ, MT = R / 16, KT = R / 16, NB = NZ / 4;
+    static constexpr int SYM = NB * (NB + 1) / 2 * 16, ASY = NB * NB * 16, BS = 4 * SYM + 2 * ASY;
+    static constexpr int MG = 3, KG = 4, MPW = MT / MG, KMAX = (KT + KG - 1) / KG;
+    static constexpr int THREADS = 32 * MG * KG;
+    static constexpr uint32_t SEG = R * 8u, XS = SEG + 32u;
+    static constexpr uint32_t G_BYTES = BS * 8u;
+    static constexpr uint32_t X_BYTES = 8u * XS;
+    static constexpr uint32_t PART_BYTES = KG * MT * 2u * 4u * 32u * 4u;
+    static constexpr uint32_t OFF_X = 2 * G_BYTES, OFF_PART = OFF_X + 2 * X_BYTES;
+    static constexpr uint32_t SMEM = OFF_PART + PART_BYTES;
+    static_assert(MT % MG == 0, "row tiles must split over the row groups");
+    static_assert(SMEM + 256 <= 227u * 1024u, "shared memory per block");
+    static_assert(MT <= MG * KG, "reduction units");
+    static_assert(BS < 0x8000, "16-bit offsets with a stride flag");
+    static_assert(G_BYTES % 128 == 0 && SEG % 16 == 0 && XS % 128 == 32, "stage alignment and bank skew");
+    __host__ __device__ static constexpr int kt0(int kg) { return kg * KT / KG; }
+};
+
+// (a, b) -> FP16 pairs hi, lo with a = hi + lo (hi rounded to 11 significant
+// bits in FP32, which FP16 holds exactly in its normal range); the low half
+// holds a (the smaller row index of the fragment)
+__device__ __forceinline__ void split_h2(float a, float b, uint32_t &hi, uint32_t &lo) {
+    const float ha = __uint_as_float(tf32_hi(__float_as_uint(a)));
+    const float hb = __uint_as_float(tf32_hi(__float_as_uint(b)));
+    const __half2 h = __floats2half2_rn(ha, hb);
+    const __half2 l = __floats2half2_rn(a - ha, b - hb);
+    hi = *reinterpret_cast<const uint32_t *>(&h);
+    lo = *reinterpret_cast<const uint32_t *>(&l);
+}
+
+__device__ __forceinline__ void mma_f16(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// offset of entry (row, col) and whether (row, col + 1) follows it directly
+// or four entries on (the transposed sub-blocks: bit 15)
+template <int NZ>
+__host__ __device__ inline uint32_t sh_entry(int row, int col) {
+    const int a = sb_index(NZ, row, col), b = sb_index(NZ, row, col + 1);
+    return (uint32_t)a | (b - a == 4 ? 0x8000u : 0u);
+}
+
+template <int NZ>
+__global__ void __launch_bounds__(Sh<NZ>::THREADS, 1)
+    k_contract_sh(float2 *buf, const float2 *__restrict__ G, const int nx, const int ny, const int B, const int rhs0,
+                  int *err) {
+    using P = Sh<NZ>;
+    constexpr int R = P::R, MPW = P::MPW, KMAX = P::KMAX;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int mg = warp % P::MG, kg = warp / P::MG;
+    const int ktb = P::kt0(kg), kcnt = P::kt0(kg + 1) - ktb;
+    int light = -1, nlight = 0;
+    {
+        int mincnt = P::KT;
+        for (int k = 0; k < P::KG; k++) mincnt = min(mincnt, P::kt0(k + 1) - P::kt0(k));
+        for (int w = 0; w < P::MG * P::KG; w++) {
+            const int wk = w / P::MG;
+            if (P::kt0(wk + 1) - P::kt0(wk) == mincnt) {
+                if (w == warp) light = nlight;
+                nlight++;
+            }
+        }
+    }
+    const uint32_t sG = saddr(smem), sX = sG + P::OFF_X;
+    const uint32_t bar0 = saddr(&bars[0]);
+    const long Q = (long)(nx + 1) * (ny + 1);
+    const int n1 = 2 * ny;
+    const int bv = g & 3, brs = g >> 2, bmx = bv >> 1, bmy = bv & 1;
+    // 1 / the split copy's scale, in its trailing entry
+    const float ginv = __uint_as_float(reinterpret_cast<const uint2 *>(G)[Q * P::BS].y);
+
+    // A-fragment entries (g, 2t), (g + 8, 2t), (g, 2t + 8), (g + 8, 2t + 8)
+    // of each (row tile, column tile) pair, two 16-bit entries per word
+    constexpr int TABN = MPW * KMAX * 2;
+    static_assert(P::MG * P::KG * TABN * 32 * 4 <= P::G_BYTES, "offset scratch must fit in one stage");
+    uint32_t tab[TABN];
+    {
+        uint32_t *scratch = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * TABN * 32 + lane;
+#pragma unroll 1
+        for (int p = 0; p < MPW * KMAX; p++) {
+            const int im = p / KMAX, ik = p - im * KMAX;
+            uint32_t w0 = 0, w1 = 0;
+            if (ik < kcnt) {
+                const int r0 = 16 * (mg * MPW + im) + g, c0 = 16 * (ktb + ik) + 2 * t;
+                w0 = sh_entry<NZ>(r0, c0) | (sh_entry<NZ>(r0 + 8, c0) << 16);
+                w1 = sh_entry<NZ>(r0, c0 + 8) | (sh_entry<NZ>(r0 + 8, c0 + 8) << 16);
+            }
+            scratch[(2 * p) * 32] = w0;
+            scratch[(2 * p + 1) * 32] = w1;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < TABN; j++) tab[j] = scratch[j * 32];
+    }
+
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    auto issue = [&](long qq, int stage) {
+        const int a = (int)(qq / (ny + 1)), bq = (int)(qq - (long)a * (ny + 1));
+        const int nkx = (a == 0 || a == nx) ? 1 : 2;
+        const int nky = (bq == 0 || bq == ny) ? 1 : 2;
+        const uint32_t bar = bar0 + 8 * stage;
+        bar_expect(bar, P::G_BYTES + (uint32_t)(nkx * nky) * (2u * P::SEG));
+        bulk_g2s(sG + stage * P::G_BYTES, G + qq * P::BS, P::G_BYTES, bar);
+        for (int p = 0; p < 4; p++) {
+            const int mx = p >> 1, my = p & 1;
+            if (mx < nkx && my < nky) {
+                const long pt = (long)(mx ? 2 * nx - a : a) * n1 + (my ? 2 * ny - bq : bq);
+#pragma unroll
+                for (int r = 0; r < 2; r++)
+                    bulk_g2s(sX + stage * P::X_BYTES + (uint32_t)(p * 2 + r) * P::XS, buf + pt * B + (long)(rhs0 + r) * R,
+                             P::SEG, bar);
+            }
+        }
+    };
+    long q = blockIdx.x;
+    if (tid == 0) {
+        // the offset scratch in stage 0 was read through the generic proxy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (q < Q) issue(q, 0);
+        if (q + gridDim.x < Q) issue(q + gridDim.x, 1);
+    }
+
+    float *PART = reinterpret_cast<float *>(smem + P::OFF_PART) + lane;
+    for (int it = 0; q < Q; q += gridDim.x, it++) {
+        const int stage = it & 1;
+        const uint32_t parity = (it >> 1) & 1;
+        const uint32_t bar = bar0 + 8 * stage;
+        const bool late = !bar_wait(bar, parity, kWait);
+        const int a = (int)(q / (ny + 1)), bq = (int)(q - (long)a * (ny + 1));
+        const int nkx = (a == 0 || a == nx) ? 1 : 2;
+        const int nky = (bq == 0 || bq == ny) ? 1 : 2;
+        const bool bpresent = bmx < nkx && bmy < nky;
+        const float4 *xcol = reinterpret_cast<const float4 *>(smem + P::OFF_X + stage * P::X_BYTES +
+                                                              (uint32_t)(bv * 2 + brs) * P::XS);
+
+        // this lane's right-hand-side values: rows 16 kt + 2t, +1 and
+        // 16 kt + 2t + 8, +9 of its column, with the D_p sign of their
+        // component and the sign of the -A^T tiles
+        float4 xv[KMAX][2];
+        float m = 0.f;
+#pragma unroll
+        for (int ik = 0; ik < KMAX; ik++) {
+            xv[ik][0] = xv[ik][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (ik < kcnt && bpresent) {
+                const int kt = ktb + ik;
+                xv[ik][0] = xcol[8 * kt + t];
+                xv[ik][1] = xcol[8 * kt + 4 + t];
+                const int comp = (16 * kt) / NZ;
+                if (((comp == 0 && bmx) || (comp == 1 && bmy)) != (mg == 2 && comp < 2)) {
+#pragma unroll
+                    for (int h = 0; h < 2; h++)
+                        xv[ik][h] = make_float4(-xv[ik][h].x, -xv[ik][h].y, -xv[ik][h].z, -xv[ik][h].w);
+                }
+#pragma unroll
+                for (int h = 0; h < 2; h++)
+                    m = fmaxf(m, fmaxf(fmaxf(fabsf(xv[ik][h].x), fabsf(xv[ik][h].y)),
+                                       fmaxf(fabsf(xv[ik][h].z), fabsf(xv[ik][h].w))));
+            }
+        }
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
+        const float scB = pow2_scale(m, 13);
+        // B fragments [ik][Xr, Xi][hi b0, hi b1, lo b0, lo b1]
+        uint32_t bf[KMAX][2][4];
+#pragma unroll
+        for (int ik = 0; ik < KMAX; ik++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float4 v = xv[ik][h];  // (re, im) of two consecutive rows
+                split_h2(v.x * scB, v.z * scB, bf[ik][0][h], bf[ik][0][2 + h]);
+                split_h2(v.y * scB, v.w * scB, bf[ik][1][h], bf[ik][1][2 + h]);
+            }
+
+        // T1 = Gr Xr, T2 = Gi Xi, T3 = Gr Xi, T4 = Gi Xr per row tile
+        float acc[MPW][4][4];
+#pragma unroll
+        for (int im = 0; im < MPW; im++)
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[im][j][c] = 0.f;
+        const uint2 *Gq = reinterpret_cast<const uint2 *>(smem + stage * P::G_BYTES);
+#pragma unroll
+        for (int ik = 0; ik < KMAX; ik++) {
+            if (ik >= kcnt) break;
+#pragma unroll
+            for (int im = 0; im < MPW; im++) {
+                // [Gr hi, Gr lo, Gi hi, Gi lo][a0..a3]
+                uint32_t af[4][4];
+                const uint32_t t0 = tab[(im * KMAX + ik) * 2], t1 = tab[(im * KMAX + ik) * 2 + 1];
+                const uint32_t ent[4] = {t0 & 0xffffu, t0 >> 16, t1 & 0xffffu, t1 >> 16};
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const uint32_t off = ent[e] & 0x7fffu, st = (ent[e] & 0x8000u) ? 4u : 1u;
+                    const uint2 u = Gq[off], w = Gq[off + st];
+                    af[0][e] = __byte_perm(u.x, w.x, 0x5410);
+                    af[2][e] = __byte_perm(u.x, w.x, 0x7632);
+                    af[1][e] = __byte_perm(u.y, w.y, 0x5410);
+                    af[3][e] = __byte_perm(u.y, w.y, 0x7632);
+                }
+                // product j: A = Gr (j even) or Gi, B = Xr (j = 0, 3) or Xi
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int ai = (j == 0 || j == 2) ? 0 : 2, bi = (j == 0 || j == 3) ? 0 : 1;
+                    mma_f16(acc[im][j], af[ai], bf[ik][bi][0], bf[ik][bi][1]);
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int ai = (j == 0 || j == 2) ? 0 : 2, bi = (j == 0 || j == 3) ? 0 : 1;
+                    mma_f16(acc[im][j], af[ai], bf[ik][bi][2], bf[ik][bi][3]);
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int ai = (j == 0 || j == 2) ? 1 : 3, bi = (j == 0 || j == 3) ? 0 : 1;
+                    mma_f16(acc[im][j], af[ai], bf[ik][bi][0], bf[ik][bi][1]);
+                }
+            }
+        }
+        // undo the scales: accumulator columns 2t and 2t + 1 carry the
+        // scales of the lanes that hold those B columns
+        const float inv = ginv / scB;
+        const float inv0 = __shfl_sync(0xffffffffu, inv, (2 * t) * 4);
+        const float inv1 = __shfl_sync(0xffffffffu, inv, (2 * t + 1) * 4);
+        __syncthreads();  // the previous point's reduction has read the partial sums
+#pragma unroll
+        for (int im = 0; im < MPW; im++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const float f = (c & 1) ? inv1 : inv0;
+                const int base = ((kg * P::MT + mg * MPW + im) * 2) * 4 + c;
+                PART[base * 32] = (acc[im][0][c] - acc[im][1][c]) * f;
+                PART[(base + 4) * 32] = (acc[im][2][c] + acc[im][3][c]) * f;
+            }
+        if (__syncthreads_or(late)) {  // partials written; the stage is free
+            if (tid == 0) {
+                atomicExch(err, EGX_ERR_TIMEOUT);
+                bar_wait(bar0 + 8 * (stage ^ 1), ((it + 1) >> 1) & 1, kWait);
+            }
+            return;
+        }
+        if (tid == 0 && q + 2L * gridDim.x < Q) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(q + 2L * gridDim.x, stage);
+        }
+        // half row tiles (rows g or g + 8) over the warps with the fewest
+        // column tiles
+        const int ubeg = light >= 0 ? light : 2 * P::MT;
+        for (int u = ubeg; u < 2 * P::MT; u += nlight) {
+            const int mt = u >> 1;
+#pragma unroll
+            for (int cc = 0; cc < 2; cc++) {
+                const int c = 2 * (u & 1) + cc;
+                float yr = 0.f, yi = 0.f;
+#pragma unroll
+                for (int k = 0; k < P::KG; k++) {
+                    const int base = ((k * P::MT + mt) * 2) * 4 + c;
+                    yr += PART[base * 32];
+                    yi += PART[(base + 4) * 32];
+                }
+                const int row = 16 * mt + g + 8 * (c >> 1);
+                const int col = 2 * t + (c & 1), v = col & 3, r = col >> 2;
+                const int mx = v >> 1, my = v & 1;
+                if (mx < nkx && my < nky) {
+                    float2 val = make_float2(yr, yi);
+                    const int comp = row / NZ;
+                    if ((comp == 0 && mx) || (comp == 1 && my)) val = make_float2(-val.x, -val.y);
+                    const long pt = (long)(mx ? 2 * nx - a : a) * n1 + (my ? 2 * ny - bq : bq);
+                    buf[pt * B + (long)(rhs0 + r) * R + row] = val;
+                }
+            }
+        }
+    }
+}
+
+template <int NZ>
+void launch_sh(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err, cudaStream_t s, int nsm) {
+    using P = Sh<NZ>;
+    raise_smem_limit((const void *)k_contract_sh<NZ>, P::SMEM);
+    const long Q = (long)(d.nx + 1) * (d.ny + 1);
+    const unsigned grid = (unsigned)std::min<long>(Q, nsm);
+    k_contract_sh<NZ><<<grid, P::THREADS, P::SMEM, s>>>(buf, G, d.nx, d.ny, d.B, rhs0, err);
+    EGX_CUDA(cudaGetLastError());
+}
+
 template <int NZ, bool BAL>
 void launch_sb3(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err, cudaStream_t s, int nsm) {
     using P = Sb3<NZ>;
@@ -685,16 +1065,17 @@ void launch_sb(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err
 
 template <int NZ>
 void launch_nz(float2 *buf, const float2 *G, const OpDims &d, int *err, cudaStream_t s, int nsm, long *launches) {
-    // contract_variant: 1 / 2 k_contract_sb3 without / with the balanced
-    // reduction, 0 the built-in choice: balanced (2.265 against 2.294 ms per
-    // two-source apply at 256x256x48, bitwise the same sums)
+    // contract_variant: 1 k_contract_sb3 (TF32 split), 2 k_contract_sh
+    // (FP16 split), 0 the built-in choice: k_contract_sh (2.059 against
+    // 2.562 ms per two-source apply at 256x256x48; 2.249 for k_contract_sb3
+    // when the copy held plain complex64)
     const int v = d.contract_variant;
     for (int r0 = 0; r0 < d.nrhs;) {
         if (d.nrhs - r0 >= 2) {
-            if (v != 1)
+            if (v == 1)
                 launch_sb3<NZ, true>(buf, G, d, r0, err, s, nsm);
             else
-                launch_sb3<NZ, false>(buf, G, d, r0, err, s, nsm);
+                launch_sh<NZ>(buf, G, d, r0, err, s, nsm);
             r0 += 2;
         } else {
             launch_sb<NZ, 1>(buf, G, d, r0, err, s, nsm);
@@ -710,14 +1091,22 @@ bool sb_layout(int nz) { return nz == 16 || nz == 32 || nz == 48; }
 
 long sb_block(int nz) { return 4L * sb_sym(nz) + 2L * sb_asy(nz); }
 
-long green_c64_entries(const GreenDims &gd) { return gd.Q() * (sb_layout(gd.nz) ? sb_block(gd.nz) : (long)gd.Bs()); }
+// the sub-block layout carries two trailing entries: the largest component
+// magnitude (and padding that keeps 16-byte multiples)
+long green_c64_entries(const GreenDims &gd) {
+    return sb_layout(gd.nz) ? gd.Q() * sb_block(gd.nz) + 2 : gd.Q() * (long)gd.Bs();
+}
 
 void green_to_c64(const double2 *g64, float2 *g32, const GreenDims &gd, cudaStream_t s, long *launches) {
     if (sb_layout(gd.nz)) {
         const long total = gd.Q() * sb_block(gd.nz);
         const unsigned blocks = (unsigned)std::min<long>((total + 255) / 256, 152L * 64);
-        k_repack_sb<<<blocks, 256, 0, s>>>(g64, g32, gd.Q(), gd.nz);
+        uint2 *g = reinterpret_cast<uint2 *>(g32);
+        EGX_CUDA(cudaMemsetAsync(g + total, 0, 2 * sizeof(uint2), s));
+        k_repack_sb<false><<<blocks, 256, 0, s>>>(g64, g, gd.Q(), gd.nz);
+        k_repack_sb<true><<<blocks, 256, 0, s>>>(g64, g, gd.Q(), gd.nz);
         EGX_CUDA(cudaGetLastError());
+        if (launches) ++*launches;
     } else {
         convert_d2f(g64, g32, gd.Q() * gd.Bs(), 1.0, s);
     }

@@ -90,11 +90,14 @@ def test_apply_small_matches_oracle(egx_ctx, small_case, op_type):
     g.free()
 
 
+@pytest.mark.parametrize("variant", [1, 2])
 @pytest.mark.parametrize("nz", [16, 32, 48])
-def test_c64_subblock_apply_matches_oracle(egx_ctx, nz):
+def test_c64_subblock_apply_matches_oracle(egx_ctx, nz, variant):
     """complex64 apply on the sub-block Green layout (nz in {16, 32, 48}),
     one to three right-hand sides (passes of two and one), ragged edges
-    (nx != ny, the kx = 0, nx and ky = 0, ny points with fewer mirrors)."""
+    (nx != ny, the kx = 0, nx and ky = 0, ny points with fewer mirrors),
+    with the two-source passes on the TF32-split (variant 1) and the
+    FP16-split (variant 2) tensor-core kernels."""
     from extreme_gb300.model import freq_to_omega, scaled_model
     m = scaled_model(10, 6, nz, seed=3)
     f = m.frequencies[2]
@@ -106,11 +109,15 @@ def test_c64_subblock_apply_matches_oracle(egx_ctx, nz):
     n = m.nx * m.ny * 3 * m.nz
     xs = rng.standard_normal((3, n)) + 1j * rng.standard_normal((3, n))
     want = [op.apply(G, om, xs[i], op.OP_A) for i in range(3)]
-    for nrhs in (1, 2, 3):
-        y = egx_ctx.op_apply_c64(xs[:nrhs].reshape(-1).astype(np.complex64), nrhs=nrhs)
-        for i in range(nrhs):
-            assert rel(y[i * n:(i + 1) * n], want[i]) < 2e-5, (nrhs, i)
-    g.free()
+    egx_ctx.apply_variant(0, variant)
+    try:
+        for nrhs in (1, 2, 3):
+            y = egx_ctx.op_apply_c64(xs[:nrhs].reshape(-1).astype(np.complex64), nrhs=nrhs)
+            for i in range(nrhs):
+                assert rel(y[i * n:(i + 1) * n], want[i]) < 2e-5, (nrhs, i)
+    finally:
+        egx_ctx.apply_variant(0, 0)
+        g.free()
 
 
 @pytest.mark.parametrize("nz,nrhs", [(48, 2), (48, 1), (7, 3), (2, 10)])
