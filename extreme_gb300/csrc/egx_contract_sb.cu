@@ -749,7 +749,10 @@ template <int NZ>
 struct Sh {
     static constexpr int R = 3 * NZ, MT = R / 16, KT = R / 16, NB = NZ / 4;
     static constexpr int SYM = NB * (NB + 1) / 2 * 16, ASY = NB * NB * 16, BS = 4 * SYM + 2 * ASY;
-    static constexpr int MG = 3, KG = 4, MPW = MT / MG, KMAX = (KT + KG - 1) / KG;
+    // 3 row groups (one component each) x 4 column groups; for nz = 32,
+    // whose 6 column tiles do not split in four, 6 x 2 (3 tiles each)
+    static constexpr int MG = NZ == 32 ? 6 : 3, KG = NZ == 32 ? 2 : 4;
+    static constexpr int MPW = MT / MG, KMAX = (KT + KG - 1) / KG;
     static constexpr int THREADS = 32 * MG * KG;
     static constexpr uint32_t SEG = R * 8u, XS = SEG + 32u;
     static constexpr uint32_t G_BYTES = BS * 8u;
@@ -760,6 +763,7 @@ struct Sh {
     static_assert(MT % MG == 0, "row tiles must split over the row groups");
     static_assert(SMEM + 256 <= 227u * 1024u, "shared memory per block");
     static_assert(MT <= MG * KG, "reduction units");
+    static_assert(NZ % (16 * MPW) == 0, "a row group within one component");
     static_assert(BS < 0x8000, "16-bit offsets with a stride flag");
     static_assert(G_BYTES % 128 == 0 && SEG % 16 == 0 && XS % 128 == 32, "stage alignment and bank skew");
     __host__ __device__ static constexpr int kt0(int kg) { return kg * KT / KG; }
@@ -823,6 +827,8 @@ __global__ void __launch_bounds__(Sh<NZ>::THREADS, 1)
     const int bv = g & 3, brs = g >> 2, bmx = bv >> 1, bmy = bv & 1;
     // 1 / the split copy's scale, in its trailing entry
     const float ginv = __uint_as_float(reinterpret_cast<const uint2 *>(G)[Q * P::BS].y);
+    // this row group's rows are z rows (its -A^T tiles take the sign)
+    const bool zrows = (16 * MPW * mg) / NZ == 2;
 
     // A-fragment entries (g, 2t), (g + 8, 2t), (g, 2t + 8), (g + 8, 2t + 8)
     // of each (row tile, column tile) pair, two 16-bit entries per word
@@ -907,7 +913,7 @@ __global__ void __launch_bounds__(Sh<NZ>::THREADS, 1)
                 xv[ik][0] = xcol[8 * kt + t];
                 xv[ik][1] = xcol[8 * kt + 4 + t];
                 const int comp = (16 * kt) / NZ;
-                if (((comp == 0 && bmx) || (comp == 1 && bmy)) != (mg == 2 && comp < 2)) {
+                if (((comp == 0 && bmx) || (comp == 1 && bmy)) != (zrows && comp < 2)) {
 #pragma unroll
                     for (int h = 0; h < 2; h++)
                         xv[ik][h] = make_float4(-xv[ik][h].x, -xv[ik][h].y, -xv[ik][h].z, -xv[ik][h].w);
