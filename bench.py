@@ -311,6 +311,9 @@ def run_ours(args, rank, world, local):
     nf3 = m.nx * m.ny * 3
     e_d = torch.empty(2 * nf3 * 2, dtype=torch.float64, device=dev)
     h_d = torch.empty_like(e_d)
+    zr_d = torch.empty(nf3 // 3 * 4 * 2, dtype=torch.float64, device=dev)
+    rho_d = torch.empty(nf3 // 3 * 4, dtype=torch.float64, device=dev)
+    ph_d = torch.empty_like(rho_d)
     pw = [egx.plane_wave(m, freq_to_omega(f), 0.0) for f in freqs]
     torch.cuda.synchronize(dev)
 
@@ -328,16 +331,22 @@ def run_ours(args, rank, world, local):
                                                       e0=e0_d[k].data_ptr(), jq=jq_d.data_ptr()))
                 ctx.level_fields_dev(m, omega, jq_d.data_ptr(), 2, e_d.data_ptr(), h_d.data_ptr(), z=0.0,
                                      precision=egx.PREC_MIXED)
-                e = e_d.cpu().numpy().view(np.complex128)
-                h = h_d.cpu().numpy().view(np.complex128)
+                # the responses at every cell centre on the device; the step's
+                # result read back is impedance, apparent resistivity and phase
+                ctx.mt_responses_dev(e_d.data_ptr(), h_d.data_ptr(), nf3 // 3, omega, pw[k][0], pw[k][1],
+                                     zr_d.data_ptr(), rho_d.data_ptr(), ph_d.data_ptr())
+                rho = rho_d.cpu().numpy().reshape(-1, 2, 2)
+                ph = ph_d.cpu().numpy().reshape(-1, 2, 2)
+                if keep is not None:
+                    e_t, h_t, _, _ = fields_and_responses(pw[k], omega, e_d.cpu().numpy().view(np.complex128),
+                                                          h_d.cpu().numpy().view(np.complex128), nf3)
+                    keep[k] = (jq_d.cpu().numpy().view(np.complex128).reshape(2, n).copy(), e_t, h_t, rho, ph)
             else:
                 z, z0 = host_in[k]
                 jq, _, res = ctx.solve_sources(g, z, z0, m.layer_thickness, host_e0[k], [0, 1],
                                                precision=egx.PREC_MIXED, mixed=mixed)
                 e, h = ctx.level_fields(m, omega, jq, z=0.0, precision=egx.PREC_MIXED)
-            out = fields_and_responses(pw[k], omega, e, h, nf3)
-            if keep is not None:
-                keep[k] = (jq_d.cpu().numpy().view(np.complex128).reshape(2, n).copy(),) + out
+                fields_and_responses(pw[k], omega, e, h, nf3)
             return res
         finally:
             g.free()
@@ -578,6 +587,9 @@ def run_plain(args, rank, world, local):
     jq_d = torch.empty(2 * n * 2, dtype=torch.float64, device=dev)
     e_d = torch.empty(2 * nf3 * 2, dtype=torch.float64, device=dev)
     h_d = torch.empty_like(e_d)
+    zr_d = torch.empty(nf3 // 3 * 4 * 2, dtype=torch.float64, device=dev)
+    rho_d = torch.empty(nf3 // 3 * 4, dtype=torch.float64, device=dev)
+    ph_d = torch.empty_like(rho_d)
     pw = [egx.plane_wave(m, freq_to_omega(f), 0.0) for f in freqs]
 
     def step(i, where):

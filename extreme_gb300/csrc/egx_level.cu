@@ -13,7 +13,9 @@
 //   inverse 2-D DFT + k_level_extract   3 columns, scaled by 1/(4 nx ny),
 //                           rows i < nx, j < ny (Plan3 backward, Zscal, ExtractData).
 // egx_mt_responses is host arithmetic on the two polarisations' total fields
-// (ResponseFunctionsCalculator.cs:36-51, PlainTextExporter.cs:322-420).
+// (ResponseFunctionsCalculator.cs:36-51, PlainTextExporter.cs:322-420);
+// egx_mt_responses_dev does the same on the device from the anomalous fields
+// that egx_level_fields_dev writes, adding the plane wave's normal field.
 #include <cmath>
 #include <complex>
 
@@ -184,6 +186,55 @@ __global__ void k_level_extract(const double2 *__restrict__ out3, int nx, int ny
     field[idx] = make_double2(scale * v.x, scale * v.y);
 }
 
+// per site: total fields of polarisation X (E + (en, 0, 0), H + (0, hn, 0))
+// and Y (E + (0, en, 0), H + (-hn, 0, 0)) from the anomalous fields [2][n][3],
+// Z = E H^-1 (2 x 2, complex128), rho = |Z|^2 / (omega mu0), phase in degrees
+__device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__global__ void k_mt_responses(const double2 *__restrict__ e, const double2 *__restrict__ h, long n, double omega,
+                               double2 en, double2 hn, double2 *__restrict__ z, double *__restrict__ rho,
+                               double *__restrict__ phase) {
+    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double2 *e1 = e + 3 * k, *e2 = e + 3 * (n + k), *h1 = h + 3 * k, *h2 = h + 3 * (n + k);
+    const double2 f11x = make_double2(e1[0].x + en.x, e1[0].y + en.y), f11y = e1[1];
+    const double2 f12x = e2[0], f12y = make_double2(e2[1].x + en.x, e2[1].y + en.y);
+    const double2 f21x = h1[0], f21y = make_double2(h1[1].x + hn.x, h1[1].y + hn.y);
+    const double2 f22x = make_double2(h2[0].x - hn.x, h2[0].y - hn.y), f22y = h2[1];
+    const double2 a = cmul2(f21x, f22y), b = cmul2(f22x, f21y);
+    const double2 det = make_double2(a.x - b.x, a.y - b.y);
+    const double dd = det.x * det.x + det.y * det.y;
+    const double2 inv = make_double2(det.x / dd, -det.y / dd);
+    const double2 hi11 = cmul2(f22y, inv), hi22 = cmul2(f21x, inv);
+    const double2 hi12 = cmul2(make_double2(-f22x.x, -f22x.y), inv), hi21 = cmul2(make_double2(-f21y.x, -f21y.y), inv);
+    double2 zz[4];
+    {
+        const double2 p = cmul2(f11x, hi11), q = cmul2(f12x, hi21);
+        zz[0] = make_double2(p.x + q.x, p.y + q.y);
+    }
+    {
+        const double2 p = cmul2(f11x, hi12), q = cmul2(f12x, hi22);
+        zz[1] = make_double2(p.x + q.x, p.y + q.y);
+    }
+    {
+        const double2 p = cmul2(f11y, hi11), q = cmul2(f12y, hi21);
+        zz[2] = make_double2(p.x + q.x, p.y + q.y);
+    }
+    {
+        const double2 p = cmul2(f11y, hi12), q = cmul2(f12y, hi22);
+        zz[3] = make_double2(p.x + q.x, p.y + q.y);
+    }
+    const double mu0 = 4.0e-7 * 3.14159265358979323846;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        z[4 * k + c] = zz[c];
+        rho[4 * k + c] = (zz[c].x * zz[c].x + zz[c].y * zz[c].y) / (omega * mu0);
+        phase[4 * k + c] = atan2(zz[c].y, zz[c].x) * (180.0 / 3.14159265358979323846);
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -323,6 +374,24 @@ int egx_level_cache(egx_ctx *ctx, int capacity, long *hits, long *builds) {
     if (hits) *hits = ctx->lvl_hits;
     if (builds) *builds = ctx->lvl_builds;
     return EGX_OK;
+}
+
+int egx_mt_responses_dev(egx_ctx *ctx, const double *e, const double *h, long n, double omega,
+                         const double e_normal[2], const double h_normal[2], double *z, double *rho, double *phase) {
+    if (!ctx) return EGX_ERR_INVALID;
+    EGX_GUARD(ctx, {
+        EGX_CHECK(e && h && e_normal && h_normal && z && rho && phase && n >= 1 && omega > 0, EGX_ERR_INVALID,
+                  "bad response arguments");
+        set_device(ctx);
+        const unsigned blocks = (unsigned)((n + 255) / 256);
+        k_mt_responses<<<blocks, 256, 0, ctx->stream>>>(
+            reinterpret_cast<const double2 *>(e), reinterpret_cast<const double2 *>(h), n, omega,
+            make_double2(e_normal[0], e_normal[1]), make_double2(h_normal[0], h_normal[1]),
+            reinterpret_cast<double2 *>(z), rho, phase);
+        EGX_CUDA(cudaGetLastError());
+        ++ctx->launches;
+        EGX_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
 }
 
 int egx_mt_responses(const double *e1, const double *e2, const double *h1, const double *h2, long n, double omega,

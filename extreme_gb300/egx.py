@@ -28,7 +28,8 @@ EXPORTS = [
     "egx_fgmres_solve", "egx_mixed_solve", "egx_set_precond", "egx_dot_products", "egx_dot_products_static",
     "egx_normal_field", "egx_plane_wave", "egx_solve_sources", "egx_profile", "egx_profile_kinds",
     "egx_profile_read",
-    "egx_level_fields", "egx_level_cache", "egx_set_level_precision", "egx_mt_responses", "egx_wait_selftest",
+    "egx_level_fields", "egx_level_cache", "egx_set_level_precision", "egx_mt_responses", "egx_mt_responses_dev",
+    "egx_wait_selftest",
     "egx_net_create", "egx_net_free", "egx_net_size", "egx_net_params", "egx_net_set_model", "egx_net_set_models", "egx_net_loss_grad",
     "egx_net_adam", "egx_net_use_tcgen05", "egx_net_apply", "egx_learned_stats", "egx_learned_inject_nonfinite",
 ]
@@ -125,6 +126,7 @@ def load(path=None):
                                       C.POINTER(Result), i]
     lib.egx_level_fields.argtypes = [vp, C.POINTER(Model), d, i, d, d, d, vp, i, vp, vp, i]
     lib.egx_mt_responses.argtypes = [vp, vp, vp, vp, C.c_long, d, vp, vp, vp]
+    lib.egx_mt_responses_dev.argtypes = [vp, vp, vp, C.c_long, d, vp, vp, vp, vp, vp]
     lib.egx_level_cache.argtypes = [vp, i, C.POINTER(C.c_long), C.POINTER(C.c_long)]
     lib.egx_set_level_precision.argtypes = [vp, i]
     lib.egx_wait_selftest.argtypes = [vp, d]
@@ -415,6 +417,17 @@ class Context:
                                               C.c_void_p(jq_ptr), nsrc, C.c_void_p(e_ptr), C.c_void_p(h_ptr),
                                               DEVICE))
 
+    def mt_responses_dev(self, e_ptr, h_ptr, n, omega, e_normal, h_normal, z_ptr, rho_ptr, ph_ptr):
+        """egx_mt_responses_dev: impedance [n][2][2] complex, apparent
+        resistivity and phase [n][2][2] into device arrays, from the anomalous
+        fields [2][n][3] on the device and the plane wave's (E, H) at the
+        level."""
+        en = np.array([complex(e_normal).real, complex(e_normal).imag])
+        hn = np.array([complex(h_normal).real, complex(h_normal).imag])
+        self._check(self.lib.egx_mt_responses_dev(self.h, C.c_void_p(e_ptr), C.c_void_p(h_ptr), int(n), float(omega),
+                                                  _ptr(en), _ptr(hn), C.c_void_p(z_ptr), C.c_void_p(rho_ptr),
+                                                  C.c_void_p(ph_ptr)))
+
     def profile(self, enable=True, kinds=None):
         """Per-kernel event timing on (the kinds listed, default all) or off."""
         mask = 0xFFFFFFFF if kinds is None else sum(1 << k for k in kinds)
@@ -428,9 +441,9 @@ class Context:
         return n.value, ms.value
 
     def set_learned(self, net):
-        """Mixed inner solves whose preconditioner is the inner GMRES cycle
-        started from the network's estimate of A^-1 v (GMRES from v as the
-        fallback); net=None goes back to the GMRES preconditioner."""
+        """Mixed inner solves with the network as their flexible
+        preconditioner (a bounded attempt, then the GMRES preconditioner as
+        the fallback); net=None goes back to the GMRES preconditioner."""
         if net is None:
             self.set_precond(PRECOND_GMRES)
         else:

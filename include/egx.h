@@ -343,6 +343,15 @@ int egx_set_level_precision(egx_ctx *ctx, int precision);
  * rho [n][4] in Ohm m, phase [n][4] in degrees. */
 int egx_mt_responses(const double *e1, const double *e2, const double *h1, const double *h2, long n, double omega,
                      double *z, double *rho, double *phase);
+/* The same responses on the device, on ctx's stream, from the anomalous
+ * fields that egx_level_fields_dev writes: e, h device arrays [2][n][3]
+ * complex (polarisations X, Y), to which the plane wave's normal field at
+ * the level is added (e_normal, h_normal: one complex value each; X:
+ * E + (en, 0, 0), H + (0, hn, 0); Y: E + (0, en, 0), H + (-hn, 0, 0), as
+ * Mt3DForwardSolver.cs:297-337 combines them). z [n][4] complex, rho [n][4],
+ * phase [n][4]: device arrays. Synchronises the stream before returning. */
+int egx_mt_responses_dev(egx_ctx *ctx, const double *e, const double *h, long n, double omega,
+                         const double e_normal[2], const double h_normal[2], double *z, double *rho, double *phase);
 
 /* ---- per-kernel device time ---------------------------------------------- */
 /* Instrumented kernels; add EGX_K_C64 for the complex64 variants. */

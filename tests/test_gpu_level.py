@@ -99,3 +99,38 @@ def test_surface_responses_match_oracle(egx_ctx):
     assert rel(lv.e[0], want["e0"]) < 10 * 1e-8 and rel(lv.h[1], want["h1"]) < 10 * 1e-8
     for a, b in ((0, 1), (1, 0)):
         assert rel(lv.rho[:, a, b], rho_w[:, a, b]) < 10 * 1e-8
+
+
+def test_device_responses_match_host(egx_ctx):
+    """egx_mt_responses_dev (device fields, the plane wave's normal field
+    added per polarisation) gives the host egx_mt_responses of the total
+    fields: impedance, apparent resistivity and phase to 1e-12."""
+    import torch
+    n = 37 * 23
+    rng = np.random.default_rng(11)
+    e = rng.standard_normal((2, n, 3)) + 1j * rng.standard_normal((2, n, 3))
+    h = rng.standard_normal((2, n, 3)) + 1j * rng.standard_normal((2, n, 3))
+    en, hn = 0.7 - 0.2j, -1.3 + 0.4j
+    omega = 2 * np.pi * 0.3
+    dev = torch.device("cuda", 0)
+    e_d = torch.from_numpy(e.reshape(-1).view(np.float64).copy()).to(dev)
+    h_d = torch.from_numpy(h.reshape(-1).view(np.float64).copy()).to(dev)
+    z_d = torch.empty(n * 4 * 2, dtype=torch.float64, device=dev)
+    rho_d = torch.empty(n * 4, dtype=torch.float64, device=dev)
+    ph_d = torch.empty(n * 4, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize(dev)
+    egx_ctx.mt_responses_dev(e_d.data_ptr(), h_d.data_ptr(), n, omega, en, hn, z_d.data_ptr(), rho_d.data_ptr(),
+                             ph_d.data_ptr())
+    et, ht = e.copy(), h.copy()
+    et[0, :, 0] += en
+    ht[0, :, 1] += hn
+    et[1, :, 1] += en
+    ht[1, :, 0] -= hn
+    z, rho, ph = egx.mt_responses(et[0], et[1], ht[0], ht[1], omega)
+    zd = z_d.cpu().numpy().view(np.complex128).reshape(n, 2, 2)
+    assert rel(zd, z) < 1e-12
+    assert rel(rho_d.cpu().numpy().reshape(n, 2, 2), rho) < 1e-12
+    np.testing.assert_allclose(ph_d.cpu().numpy().reshape(n, 2, 2), ph, rtol=0, atol=1e-9)
+    with pytest.raises(egx.EgxError):
+        egx_ctx.mt_responses_dev(e_d.data_ptr(), h_d.data_ptr(), 0, omega, en, hn, z_d.data_ptr(),
+                                 rho_d.data_ptr(), ph_d.data_ptr())
