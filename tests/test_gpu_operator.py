@@ -148,3 +148,26 @@ def test_apply_before_prepare_is_state_error():
         ctx.op_apply(np.zeros(24, complex))
     assert e.value.code == egx.ERR_STATE
     ctx.close()
+
+
+def test_c64_apply_512_point_lines_match_complex128(egx_ctx):
+    """The complex64 apply with 512-point lines in both directions (the
+    two-pass register FFT of 32 x 16 points) against the complex128 apply
+    of the same operator (three-pass FFT) on the device, 256x256x16, two
+    right-hand sides: complex64 accuracy."""
+    from extreme_gb300.model import freq_to_omega, scaled_model
+    m = scaled_model(256, 256, 16, seed=4)
+    f = m.frequencies[1]
+    om = OmegaModel.build(m, f)
+    g = egx_ctx.green_build(m, freq_to_omega(f), 10, egx.PREC_MIXED)
+    try:
+        egx_ctx.op_prepare(g, om.zeta, om.zeta0, m.layer_thickness, op.OP_A)
+        rng = np.random.default_rng(16)
+        n = m.nx * m.ny * 3 * m.nz
+        xs = rng.standard_normal((2, n)) + 1j * rng.standard_normal((2, n))
+        y32 = egx_ctx.op_apply_c64(xs.reshape(-1).astype(np.complex64), nrhs=2)
+        for i in range(2):
+            y64 = egx_ctx.op_apply(xs[i])
+            assert rel(y32[i * n:(i + 1) * n], y64) < 2e-6, i
+    finally:
+        g.free()
