@@ -134,12 +134,13 @@ int egx_graph_stats(egx_ctx *ctx, long *replays, long *nodes);
 /* Apply autotuner (no reference counterpart): on the prepared operator
  * (complex64 Green tensor), times `reps` complex64 applies of nrhs vectors
  * for every kernel variant -- the FFT passes' column tile (0 built-in per
- * pass, 1 64-byte, 2 128-byte) x the contraction kernel of the packed Green
- * layout (0 built-in order, 1 TMA-staged CUDA-core, 2 generic; the sub-block
- * layout of nz in {16, 32, 48} has one) -- keeps the fastest for the
- * context's later complex64 applies, and writes the mean ms per apply to
- * ms_out[tile * 3 + variant] (9 doubles, -1 where not applicable; may be
- * NULL). The results do not depend on the choice. */
+ * pass, 1 64-byte, 2 128-byte) x the contraction kernel: for the packed
+ * Green layout 0 built-in order, 1 TMA-staged CUDA-core, 2 generic; for the
+ * sub-block layout of nz in {16, 32, 48} 0 built-in (FP16 split), 1 TF32
+ * split, 2 FP16 split -- keeps the fastest for the context's later
+ * complex64 applies, and writes the mean ms per apply to
+ * ms_out[tile * 3 + variant] (9 doubles; may be NULL). The results agree to
+ * complex64 rounding whatever the choice. */
 int egx_tune_apply(egx_ctx *ctx, int nrhs, int reps, double *ms_out);
 /* Set the variants by hand (same ranges). */
 int egx_apply_variant(egx_ctx *ctx, int fft_tile, int contract_variant);
