@@ -92,7 +92,7 @@ def counts_method(workload):
     return dict(m_out=20, m_in=10, tol=1e-8, max_restarts=100), "complex128 FGMRES(20) + GMRES(10), tol 1e-8"
 
 
-# FP64 peak of one GB300 (nominal; the driver's measured peaks cover HBM and
+# FP64 peak of one GB300 (nominal; the measured peaks file covers HBM and
 # bf16 only): the bound of the plain complex128 apply.
 FP64_PEAK_GFLOPS_NOMINAL = 1250.0
 
