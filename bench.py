@@ -315,6 +315,20 @@ def run_ours(args, rank, world, local):
     rho_d = torch.empty(nf3 // 3 * 4, dtype=torch.float64, device=dev)
     ph_d = torch.empty_like(rho_d)
     pw = [egx.plane_wave(m, freq_to_omega(f), 0.0) for f in freqs]
+
+    # page-locked host buffers of the end-to-end steps: the inputs as a caller
+    # holds them, jQ and the surface fields written in place by the library
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.complex128, pin_memory=True).numpy()
+
+    pin_in, pin_e0 = [], []
+    for (z, z0), e in zip(host_in, host_e0):
+        pz, pz0, pe = pinned(z.shape), pinned(z0.shape), pinned(e.shape)
+        pz[...], pz0[...], pe[...] = z, z0, e
+        pin_in.append((pz, pz0))
+        pin_e0.append(pe)
+    pin_jq = pinned((2, n))
+    pin_eh = (pinned((2, m.nx, m.ny, 3)), pinned((2, m.nx, m.ny, 3)))
     torch.cuda.synchronize(dev)
 
     def step(i, where, keep=None):
@@ -342,10 +356,10 @@ def run_ours(args, rank, world, local):
                                                           h_d.cpu().numpy().view(np.complex128), nf3)
                     keep[k] = (jq_d.cpu().numpy().view(np.complex128).reshape(2, n).copy(), e_t, h_t, rho, ph)
             else:
-                z, z0 = host_in[k]
-                jq, _, res = ctx.solve_sources(g, z, z0, m.layer_thickness, host_e0[k], [0, 1],
-                                               precision=egx.PREC_MIXED, mixed=mixed)
-                e, h = ctx.level_fields(m, omega, jq, z=0.0, precision=egx.PREC_MIXED)
+                z, z0 = pin_in[k]
+                jq, _, res = ctx.solve_sources(g, z, z0, m.layer_thickness, pin_e0[k], [0, 1],
+                                               precision=egx.PREC_MIXED, mixed=mixed, out=pin_jq)
+                e, h = ctx.level_fields(m, omega, jq, z=0.0, precision=egx.PREC_MIXED, out=pin_eh)
                 fields_and_responses(pw[k], omega, e, h, nf3)
             return res
         finally:
@@ -401,8 +415,11 @@ def run_ours(args, rank, world, local):
     e1_ev.record(stream)
     barrier()
     ms_e2e = max(e0_ev.elapsed_time(e1_ev), (time.perf_counter() - t1) * 1e3)
-    h2d = m.nx * m.ny * m.nz * 16 + m.nz * 16 + m.nz * 8 + 2 * m.nz * 16
-    d2h = 2 * 2 * nf3 * 16   # E and H of both polarisations at the surface
+    # in: zeta, zeta0, dz, the two normal-field columns, and jQ of both
+    # polarisations back in for the level fields; out: jQ, then E and H of
+    # both polarisations at the surface
+    h2d = m.nx * m.ny * m.nz * 16 + m.nz * 16 + m.nz * 8 + 2 * m.nz * 16 + 2 * n * 16
+    d2h = 2 * n * 16 + 2 * 2 * nf3 * 16
 
     # ---- plain FP64 (the reference algorithm, its defaults, tol 1e-6) at
     # frequency index 1; its device-built complex128 tensor is kept on the

@@ -335,11 +335,13 @@ class Context:
                                                      C.c_void_p(out_ptr)))
 
     def solve_sources(self, green, zeta, zeta0, dz, e0, pols, precision=PREC_FP64, fgmres=None, mixed=None,
-                      want_chi=False, where=HOST, dev_ptrs=None):
+                      want_chi=False, where=HOST, dev_ptrs=None, out=None):
         """SolveForOneSource up to jQ for each (e0[i], pols[i]).
 
         Host mode: zeta [nx,ny,nz], zeta0 [nz], e0 [nsrc, nz] complex128 arrays;
-        returns (jq [nsrc, N], chi or None, [result dicts]).
+        returns (jq [nsrc, N], chi or None, [result dicts]); out: a
+        C-contiguous complex128 host array of nsrc * N entries for jq (e.g.
+        page-locked).
         Device mode: dev_ptrs = dict(zeta=, zeta0=, e0=, jq=, chi=) device pointers."""
         nsrc = len(pols)
         pol = np.ascontiguousarray(pols, np.int32)
@@ -366,7 +368,13 @@ class Context:
         z0 = _c128(zeta0)
         e = _c128(e0).reshape(nsrc, -1)
         n = z.size * 3
-        jq = np.empty((nsrc, n), np.complex128)
+        if out is not None:
+            jq = out
+            if jq.dtype != np.complex128 or not jq.flags.c_contiguous or jq.size != nsrc * n:
+                raise ValueError("out must be a C-contiguous complex128 array of %d entries" % (nsrc * n))
+            jq = jq.reshape(nsrc, n)
+        else:
+            jq = np.empty((nsrc, n), np.complex128)
         chi = np.empty((nsrc, n), np.complex128) if want_chi else None
         rc = self.lib.egx_solve_sources(self.h, green.h, _ptr(z), _ptr(z0), _ptr(dz), _ptr(e), _ptr(pol), nsrc,
                                         C.byref(p), _ptr(chi) if want_chi else None, _ptr(jq), res, HOST)
@@ -394,15 +402,25 @@ class Context:
         level tensors) for the level tensors built from now on."""
         self._check(self.lib.egx_set_level_precision(self.h, int(precision)))
 
-    def level_fields(self, model, omega, jq, z=0.0, shift_x=0.0, shift_y=0.0, n_hankels=10, precision=PREC_FP64):
+    def level_fields(self, model, omega, jq, z=0.0, shift_x=0.0, shift_y=0.0, n_hankels=10, precision=PREC_FP64,
+                     out=None):
         """Anomalous E and H at the observation level z for jq [nsrc, N]
         (host arrays): returns (e, h), each [nsrc, nx, ny, 3] complex128.
-        precision: of the level tensors (egx_set_level_precision)."""
+        precision: of the level tensors (egx_set_level_precision). out: an
+        (e, h) pair of C-contiguous complex128 host arrays of that shape to
+        write into (e.g. page-locked buffers)."""
         self.set_level_precision(precision)
         jq = _c128(jq).reshape(-1, model.nx * model.ny * 3 * model.nz)
         nsrc = jq.shape[0]
-        e = np.empty((nsrc, model.nx, model.ny, 3), np.complex128)
-        h = np.empty_like(e)
+        if out is not None:
+            e, h = out
+            shape = (nsrc, model.nx, model.ny, 3)
+            for a in (e, h):
+                if a.dtype != np.complex128 or not a.flags.c_contiguous or a.size != int(np.prod(shape)):
+                    raise ValueError("out arrays must be C-contiguous complex128 of %s" % (shape,))
+        else:
+            e = np.empty((nsrc, model.nx, model.ny, 3), np.complex128)
+            h = np.empty_like(e)
         ms = model_struct(model)
         self._check(self.lib.egx_level_fields(self.h, C.byref(ms.s), omega, n_hankels, z, shift_x, shift_y,
                                               _ptr(jq), nsrc, _ptr(e), _ptr(h), HOST))

@@ -46,6 +46,38 @@ def test_level_fields_match_oracle(egx_ctx, z, sx, sy):
         assert rel(h[i], atoo.anomaly_field(om, gh, jq[i], "H")) < 1e-10, (i, "H")
 
 
+def test_host_out_buffers_page_locked(egx_ctx):
+    """Caller-supplied page-locked host outputs: jQ of the solve and the level
+    fields written in place, equal to the allocating calls; a wrong dtype or
+    size raises before anything runs."""
+    import torch
+    m, om = _tiny()
+    n = m.nx * m.ny * 3 * m.nz
+    g = egx_ctx.green_build(m, om.omega, 10)
+    try:
+        from extreme_gb300.forward import model_zeta
+        zeta = model_zeta(m, om.omega)
+        e0 = np.stack([egx.normal_field(m, om.omega)] * 2)
+        kw = dict(fgmres=dict(m_out=15, m_in=10, tol=1e-8, max_restarts=50))
+        jq_a, _, _ = egx_ctx.solve_sources(g, zeta[0], zeta[1], m.layer_thickness, e0, [0, 1], **kw)
+        pin_jq = torch.empty((2, n), dtype=torch.complex128, pin_memory=True).numpy()
+        jq_b, _, _ = egx_ctx.solve_sources(g, zeta[0], zeta[1], m.layer_thickness, e0, [0, 1], out=pin_jq, **kw)
+        assert jq_b.ctypes.data == pin_jq.ctypes.data
+        assert rel(pin_jq, jq_a) < 1e-12
+        with pytest.raises(ValueError):
+            egx_ctx.solve_sources(g, zeta[0], zeta[1], m.layer_thickness, e0, [0, 1],
+                                  out=np.empty((2, n), np.complex64), **kw)
+    finally:
+        g.free()
+    e_a, h_a = egx_ctx.level_fields(m, om.omega, jq_a, z=0.0)
+    pin = tuple(torch.empty((2, m.nx, m.ny, 3), dtype=torch.complex128, pin_memory=True).numpy() for _ in range(2))
+    e_b, h_b = egx_ctx.level_fields(m, om.omega, pin_jq, z=0.0, out=pin)
+    assert e_b is pin[0] and h_b is pin[1]
+    assert rel(pin[0], e_a) < 1e-12 and rel(pin[1], h_a) < 1e-12
+    with pytest.raises(ValueError):
+        egx_ctx.level_fields(m, om.omega, jq_a, z=0.0, out=(pin[0][:1], pin[1]))
+
+
 @pytest.mark.parametrize("shape", [(8, 6, 3), (32, 32, 8)])
 def test_mixed_level_tensors_match_fp64(egx_ctx, shape):
     """Level tensors with the complex64 lateral FFT (the mixed form): fields
