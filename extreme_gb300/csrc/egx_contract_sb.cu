@@ -781,6 +781,14 @@ __device__ __forceinline__ void split_h2(float a, float b, uint32_t &hi, uint32_
     lo = *reinterpret_cast<const uint32_t *>(&l);
 }
 
+// d = a b (zero accumulator)
+__device__ __forceinline__ void mma_f16_zero(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%10,%10,%10,%10};"
+        : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1), "f"(0.f));
+}
+
 __device__ __forceinline__ void mma_f16(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
     asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
         "{%0,%1,%2,%3};"
@@ -862,7 +870,7 @@ __global__ void __launch_bounds__(Sh<NZ>::THREADS, 1)
     __syncthreads();
 
     auto issue = [&](long qq, int stage) {
-        const int a = (int)(qq / (ny + 1)), bq = (int)(qq - (long)a * (ny + 1));
+        const int a = (int)((unsigned)qq / (unsigned)(ny + 1)), bq = (int)qq - a * (ny + 1);
         const int nkx = (a == 0 || a == nx) ? 1 : 2;
         const int nky = (bq == 0 || bq == ny) ? 1 : 2;
         const uint32_t bar = bar0 + 8 * stage;
@@ -893,7 +901,8 @@ __global__ void __launch_bounds__(Sh<NZ>::THREADS, 1)
         const uint32_t parity = (it >> 1) & 1;
         const uint32_t bar = bar0 + 8 * stage;
         const bool late = !bar_wait(bar, parity, kWait);
-        const int a = (int)(q / (ny + 1)), bq = (int)(q - (long)a * (ny + 1));
+        // Q < 2^31 (checked at launch): 32-bit point decoding
+        const int a = (int)((unsigned)q / (unsigned)(ny + 1)), bq = (int)q - a * (ny + 1);
         const int nkx = (a == 0 || a == nx) ? 1 : 2;
         const int nky = (bq == 0 || bq == ny) ? 1 : 2;
         const bool bpresent = bmx < nkx && bmy < nky;
@@ -939,13 +948,16 @@ __global__ void __launch_bounds__(Sh<NZ>::THREADS, 1)
             }
 
         // T1 = Gr Xr, T2 = Gi Xi, T3 = Gr Xi, T4 = Gi Xr per row tile
+        // (the first k tile's first products start from zero accumulators)
         float acc[MPW][4][4];
+        if (kcnt <= 0) {
 #pragma unroll
-        for (int im = 0; im < MPW; im++)
+            for (int im = 0; im < MPW; im++)
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+                for (int j = 0; j < 4; j++)
 #pragma unroll
-                for (int c = 0; c < 4; c++) acc[im][j][c] = 0.f;
+                    for (int c = 0; c < 4; c++) acc[im][j][c] = 0.f;
+        }
         const uint2 *Gq = reinterpret_cast<const uint2 *>(smem + stage * P::G_BYTES);
 #pragma unroll
         for (int ik = 0; ik < KMAX; ik++) {
@@ -969,7 +981,8 @@ __global__ void __launch_bounds__(Sh<NZ>::THREADS, 1)
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const int ai = (j == 0 || j == 2) ? 0 : 2, bi = (j == 0 || j == 3) ? 0 : 1;
-                    mma_f16(acc[im][j], af[ai], bf[ik][bi][0], bf[ik][bi][1]);
+                    if (ik == 0) mma_f16_zero(acc[im][j], af[ai], bf[ik][bi][0], bf[ik][bi][1]);
+                    else mma_f16(acc[im][j], af[ai], bf[ik][bi][0], bf[ik][bi][1]);
                 }
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
@@ -1044,6 +1057,7 @@ void launch_sh(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err
     using P = Sh<NZ>;
     raise_smem_limit((const void *)k_contract_sh<NZ>, P::SMEM);
     const long Q = (long)(d.nx + 1) * (d.ny + 1);
+    EGX_CHECK(Q < (1L << 31), EGX_ERR_INVALID, "sub-block contraction: (nx + 1)(ny + 1) must be below 2^31");
     const unsigned grid = (unsigned)std::min<long>(Q, nsm);
     k_contract_sh<NZ><<<grid, P::THREADS, P::SMEM, s>>>(buf, G, d.nx, d.ny, d.B, rhs0, err);
     EGX_CUDA(cudaGetLastError());
