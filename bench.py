@@ -11,9 +11,9 @@ all 256x256 cell centres. Steps cycle over the model's four frequencies
 (1e-3 .. 10 Hz, log-spaced).
 
 Keys of the JSON line beyond the common ones:
-  e2e          the same solves through the C ABI with host buffers
-               (zeta, zeta0, dz, E0 copied in; surface E and H of both
-               polarisations out);
+  e2e          the same solves through the C ABI with page-locked host
+               buffers (zeta, zeta0, dz, E0 in; jQ of both polarisations out
+               and back in for the level fields; surface E and H out);
   roofline     the complex64 block-contraction kernel, its CUDA-event time on
                the library's stream during the timed region, against the
                measured HBM copy bandwidth; roofline.apply: the whole
@@ -470,7 +470,7 @@ def run_ours(args, rank, world, local):
     peak, peak_src = load_peaks()
     achieved = alg_bytes / (kms / kc / 1e3) / 1e9 if kc else None
     if m.nz in (16, 32, 48):
-        kname = "k_contract_sh" if rhs == 2 else "k_contract_sb"
+        kname = "k_contract_ws" if rhs == 2 else "k_contract_sb"
     else:  # packed layout: the tensor-core kernel takes one source, the TMA kernel two
         kname = "k_contract_c64" if rhs == 2 else "k_contract_mma"
     roofline = {"kernel": kname, "bound": "hbm", "rhs_per_launch": rhs,

@@ -6,11 +6,14 @@
 // Sub-block layout of one stored spectral point (nb = nz/4):
 //   xx | xy | yy | zz : the nb(nb+1)/2 upper-triangle 4x4 sub-blocks (I <= J)
 //                       of the symmetric block, sub-block I + J(J+1)/2,
-//                       element (i%4)*4 + (j%4); diagonal sub-blocks whole;
+//                       element (i%4)*4 + (j%4) ^ sb_swz(I, J); diagonal
+//                       sub-blocks whole;
 //   xz | yz           : all nb*nb sub-blocks, sub-block I*nb + J, element
-//                       (rc%4)*4 + (tr%4).
-// Every fragment load of a half-warp (4 rows x 4 columns of G, either
-// orientation) then falls in one 128-byte sub-block: conflict-free.
+//                       (rc%4)*4 + (tr%4) ^ sb_swz(I, J).
+// A TF32 fragment load of a half-warp (4 rows x 4 columns of G, either
+// orientation) falls in one 128-byte sub-block; the FP16 kernels' loads of
+// entry pairs span two adjacent sub-blocks, which the sb_swz checkerboard
+// sends to different banks: both conflict-free.
 //
 // Each 8-byte entry holds the Green value scaled by one power of two for
 // the whole tensor and split into FP16 high parts and remainders of Re and
@@ -22,20 +25,21 @@
 // of split operands takes three MMAs (hi.hi + hi.lo + lo.hi), which keeps
 // complex64 accuracy.
 //
-// Work split per CTA (one per SM, loop over stored points): 12 warps as
-// 3 row groups x 4 column groups; each warp owns 1/3 of the 16-row tiles and
-// a quarter of the column tiles, keeps the offsets of its A fragments in
-// registers (built once), and accumulates partial products per row tile.
-// The -A^T blocks (z rows, x|y columns) are exactly the tiles of row group 2
-// and the x|y column tiles, so their sign goes onto those warps' B values.
-// The column groups' partial sums meet in shared memory and are added and
-// stored by the warps with the fewest column tiles.
-//
-// Three kernels: k_contract_sh<NZ> for two right-hand sides (the stacked
-// solve of both polarisations: FP16 m16n8k16, A fragments straight from the
-// split entries), k_contract_sb3<NZ> for two on the TF32 m16n8k8 path (the
-// entries recombined to complex64 first; the tuner's alternative), and
-// k_contract_sb<NZ, 1> for one (TF32, recombined entries).
+// Four kernels, one CTA per SM looping over stored points, the offsets of
+// each warp's A fragments held in registers (built once). The -A^T blocks
+// (z rows, x|y columns) take their sign on the B values.
+//  * k_contract_ws<NZ> (two right-hand sides, the stacked solve of both
+//    polarisations; built in): FP16 m16n8k16 with A fragments straight from
+//    the split entries, work split by role -- one warp per 16-row tile over
+//    all column tiles, two warps splitting the next point's right-hand
+//    sides, one producer lane (see the kernel).
+//  * k_contract_sh<NZ> (two; the tuner's variant 2): the same products with
+//    12 warps in lockstep, 3 row groups x 4 column groups, partial sums per
+//    row tile met in shared memory and added by the warps with the fewest
+//    column tiles.
+//  * k_contract_sb3<NZ> (two; variant 1) on the TF32 m16n8k8 path, the
+//    entries recombined to complex64 first, and k_contract_sb<NZ, 1> for one
+//    right-hand side.
 //
 // Per stored point: one TMA bulk copy of the block and one per present
 // right-hand-side segment into one of two stages, issued two points ahead
@@ -143,6 +147,16 @@ constexpr uint64_t kWait = 2000000000ull;
 __host__ __device__ inline int sb_sym(int nz) { return (nz / 4) * (nz / 4 + 1) / 2 * 16; }
 __host__ __device__ inline int sb_asy(int nz) { return (nz / 4) * (nz / 4) * 16; }
 
+// Entry (a, b) of the stored 4x4 sub-block (I, J) of a component block sits
+// at a * 4 + b XOR sb_swz(I, J): a checkerboard over the sub-blocks that
+// sends the FP16 kernels' A-fragment loads of two horizontally adjacent
+// sub-blocks (read in place) to the even and the odd entries, and those of
+// two vertically adjacent ones (read transposed) to entries 0-3, 8-11 and
+// 4-7, 12-15 -- different banks, where the plain order put both on the
+// same ones. The neighbour (a, b + 1) of an entry with b even is then at
+// index ^ 1, the neighbour (a + 1, b) of one with a even at index ^ 4.
+__host__ __device__ inline int sb_swz(int I, int J) { return (J & 1) | ((I & 1) << 2); }
+
 // index in the sub-block layout of the entry G(row, col) of the 3nz x 3nz
 // point operator, up to the sign of the -A^T blocks
 __host__ __device__ inline int sb_index(int nz, int row, int col) {
@@ -159,10 +173,31 @@ __host__ __device__ inline int sb_index(int nz, int row, int col) {
             a = b;
             b = s;
         }
-        return c * S + (I + J * (J + 1) / 2) * 16 + a * 4 + b;
+        return c * S + (I + J * (J + 1) / 2) * 16 + ((a * 4 + b) ^ sb_swz(I, J));
     }
-    if (ci == 2) return 4 * S + co * A + ((i >> 2) * nb + (j >> 2)) * 16 + (i & 3) * 4 + (j & 3);
-    return 4 * S + ci * A + ((j >> 2) * nb + (i >> 2)) * 16 + (j & 3) * 4 + (i & 3);
+    if (ci == 2)
+        return 4 * S + co * A + ((i >> 2) * nb + (j >> 2)) * 16 + (((i & 3) * 4 + (j & 3)) ^ sb_swz(i >> 2, j >> 2));
+    return 4 * S + ci * A + ((j >> 2) * nb + (i >> 2)) * 16 + (((j & 3) * 4 + (i & 3)) ^ sb_swz(j >> 2, i >> 2));
+}
+
+// the inverse for the repack: index d of the sub-block layout -> index of
+// its entry in the packed complex128 quadrant (GreenDims: a packed triangle
+// S0 per symmetric component, rows of xz and yz padded to nz + 1)
+__host__ __device__ inline int sb_packed_source(int nz, int d) {
+    const int S = sb_sym(nz), A = sb_asy(nz), nb = nz / 4;
+    const int S0 = nz * (nz + 1) / 2, lda = nz + 1, A0 = nz * lda;
+    if (d < 4 * S) {
+        const int c = d / S, r = d - c * S, sbi = r >> 4;
+        int J = 0;
+        while ((J + 1) * (J + 2) / 2 <= sbi) J++;
+        const int I = sbi - J * (J + 1) / 2, e = (r & 15) ^ sb_swz(I, J);
+        const int i = 4 * I + (e >> 2), j = 4 * J + (e & 3);
+        const int lo = i < j ? i : j, hi = i < j ? j : i;
+        return c * S0 + lo + hi * (hi + 1) / 2;
+    }
+    const int d2 = d - 4 * S, co = d2 / A, r = d2 - co * A, sbi = r >> 4;
+    const int I = sbi / nb, J = sbi - I * nb, e = (r & 15) ^ sb_swz(I, J);
+    return 4 * S0 + co * A0 + (4 * I + (e >> 2)) * lda + 4 * J + (e & 3);
 }
 
 // complex128 packed quadrant (GreenDims layout) -> the split sub-block copy.
@@ -174,7 +209,7 @@ __host__ __device__ inline int sb_index(int nz, int row, int col) {
 // copy's trailing entry, g32[Q BS].
 template <bool WRITE>
 __global__ void k_repack_sb(const double2 *__restrict__ g64, uint2 *__restrict__ g32, long Q, int nz) {
-    const int S = sb_sym(nz), A = sb_asy(nz), BS = 4 * S + 2 * A, nb = nz / 4;
+    const int S = sb_sym(nz), A = sb_asy(nz), BS = 4 * S + 2 * A;
     // packed layout (GreenDims): S0 per symmetric block, rows of xz/yz padded to nz + 1
     const int S0 = nz * (nz + 1) / 2, lda = nz + 1, A0 = nz * lda, BS0 = 4 * S0 + 2 * A0;
     const long total = Q * BS;
@@ -188,21 +223,7 @@ __global__ void k_repack_sb(const double2 *__restrict__ g64, uint2 *__restrict__
     for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
         const long q = idx / BS;
         const int d = (int)(idx - q * BS);
-        int src;
-        if (d < 4 * S) {
-            const int c = d / S, r = d - c * S, sbi = r >> 4, e = r & 15;
-            int J = 0;
-            while ((J + 1) * (J + 2) / 2 <= sbi) J++;
-            const int I = sbi - J * (J + 1) / 2;
-            const int i = 4 * I + (e >> 2), j = 4 * J + (e & 3);
-            const int lo = i < j ? i : j, hi = i < j ? j : i;
-            src = c * S0 + lo + hi * (hi + 1) / 2;
-        } else {
-            const int d2 = d - 4 * S, co = d2 / A, r = d2 - co * A, sbi = r >> 4, e = r & 15;
-            const int I = sbi / nb, J = sbi - I * nb;
-            src = 4 * S0 + co * A0 + (4 * I + (e >> 2)) * lda + 4 * J + (e & 3);
-        }
-        const double2 v = g64[q * BS0 + src];
+        const double2 v = g64[q * BS0 + sb_packed_source(nz, d)];
         if (WRITE)
             g32[idx] = split_entry((float)(v.x * scale), (float)(v.y * scale));
         else
@@ -796,12 +817,12 @@ __device__ __forceinline__ void mma_f16(float *c, const uint32_t *a, uint32_t b0
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// offset of entry (row, col) and whether (row, col + 1) follows it directly
-// or four entries on (the transposed sub-blocks: bit 15)
+// offset of entry (row, col), col even, and whether (row, col + 1) sits at
+// offset ^ 1 or, in the transposed sub-blocks, at offset ^ 4 (bit 15)
 template <int NZ>
 __host__ __device__ inline uint32_t sh_entry(int row, int col) {
     const int a = sb_index(NZ, row, col), b = sb_index(NZ, row, col + 1);
-    return (uint32_t)a | (b - a == 4 ? 0x8000u : 0u);
+    return (uint32_t)a | ((a ^ b) == 4 ? 0x8000u : 0u);
 }
 
 template <int NZ>
@@ -970,8 +991,8 @@ __global__ void __launch_bounds__(Sh<NZ>::THREADS, 1)
                 const uint32_t ent[4] = {t0 & 0xffffu, t0 >> 16, t1 & 0xffffu, t1 >> 16};
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
-                    const uint32_t off = ent[e] & 0x7fffu, st = (ent[e] & 0x8000u) ? 4u : 1u;
-                    const uint2 u = Gq[off], w = Gq[off + st];
+                    const uint32_t off = ent[e] & 0x7fffu, nb = (ent[e] & 0x8000u) ? 4u : 1u;
+                    const uint2 u = Gq[off], w = Gq[off ^ nb];
                     af[0][e] = __byte_perm(u.x, w.x, 0x5410);
                     af[2][e] = __byte_perm(u.x, w.x, 0x7632);
                     af[1][e] = __byte_perm(u.y, w.y, 0x5410);
@@ -1052,6 +1073,298 @@ __global__ void __launch_bounds__(Sh<NZ>::THREADS, 1)
     }
 }
 
+// k_contract_ws<NZ>: the two-source FP16 split contraction with its work
+// split by role, so that the phases of one point overlap the products of
+// another instead of running in lockstep behind block barriers.
+//  * MMA warps, one per row tile (MT of them): every k tile of their tile,
+//    12 products per k tile as in k_contract_sh, accumulators alternating
+//    by k tile; the output leaves from the accumulators (no partial sums).
+//  * two split warps: load the right-hand sides of a point from global
+//    memory (the Green stage carries no right-hand sides), take one scale
+//    per column over all its rows, split into FP16 fragments in a double
+//    buffer, while the MMA warps work on the point before.
+//  * one producer lane: a TMA bulk copy of the next Green block into the
+//    stage the MMA warps released.
+// Hand-offs are mbarriers; every wait is bounded, and a wait that gives up
+// records EGX_ERR_TIMEOUT and raises a block-wide abort flag that ends every
+// role's loop within one poll.
+template <int NZ>
+struct Ws {
+    static constexpr int R = 3 * NZ, MT = R / 16, KT = R / 16, BS = Sh<NZ>::BS;
+    static constexpr int NSPLIT = 2, PRODUCER = MT + NSPLIT, THREADS = 32 * (MT + NSPLIT + 1);
+    static constexpr int KPS = (KT + NSPLIT - 1) / NSPLIT;  // k tiles per split warp
+    static constexpr uint32_t G_BYTES = BS * 8u;
+    static constexpr uint32_t BF_BYTES = KT * 2u * 32u * 16u;  // [KT][Xr, Xi][32 lanes] uint4
+    static constexpr uint32_t OFF_BF = 2 * G_BYTES, OFF_INV = OFF_BF + 2 * BF_BYTES;
+    static constexpr uint32_t OFF_MAX = OFF_INV + 2u * 8u * 4u;
+    static constexpr uint32_t SMEM = OFF_MAX + 2u * NSPLIT * 8u * 4u;
+    static_assert(SMEM + 256 <= 227u * 1024u, "shared memory per block");
+    static_assert(MT * KT * 2 * 32 * 4 <= G_BYTES, "offset scratch must fit in one stage");
+    static_assert(G_BYTES % 128 == 0 && OFF_BF % 16 == 0, "stage alignment");
+};
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// bounded wait that also ends once another thread of the block gave up
+__device__ __forceinline__ bool ws_wait(uint32_t bar, uint32_t parity, volatile int *abort, int *err) {
+    const uint64_t t0 = wait_clock_ns();
+    while (!mbar_try_parity(bar, parity)) {
+        if (*abort) return false;
+        if (wait_clock_ns() - t0 > kWait) {
+            *abort = 1;
+            atomicExch(err, EGX_ERR_TIMEOUT);
+            return false;
+        }
+    }
+    return true;
+}
+
+// the same for all 32 lanes of a warp, which leave or go on together (the
+// MMA and shuffle code after it needs the whole warp)
+__device__ __forceinline__ bool ws_wait_warp(uint32_t bar, uint32_t parity, volatile int *abort, int *err) {
+    const bool ok = ws_wait(bar, parity, abort, err);
+    return __all_sync(0xffffffffu, ok);
+}
+
+template <int NZ>
+__global__ void __launch_bounds__(Ws<NZ>::THREADS, 1)
+    k_contract_ws(float2 *buf, const float2 *__restrict__ G, const int nx, const int ny, const int B, const int rhs0,
+                  int *err) {
+    using P = Ws<NZ>;
+    constexpr int R = P::R, KT = P::KT;
+    extern __shared__ __align__(128) unsigned char smem[];
+    // [full, sempty, bfull, bempty, cmax] x 2: Green block landed, stage
+    // read, fragments split, fragments read, split warps' column maxima
+    __shared__ __align__(8) uint64_t bars[10];
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const uint32_t sG = saddr(smem);
+    const uint32_t b_full = saddr(&bars[0]), b_sempty = b_full + 16, b_bfull = b_full + 32;
+    const uint32_t b_bempty = b_full + 48, b_max = b_full + 64;
+    volatile int *abort = &abort_flag;
+    const int Q = (nx + 1) * (ny + 1);  // below 2^31, checked at launch
+    const int n1 = 2 * ny;
+    // 1 / the split copy's scale, in its trailing entry
+    const float ginv = __uint_as_float(reinterpret_cast<const uint2 *>(G)[(long)Q * P::BS].y);
+    uint4 *BFRAG = reinterpret_cast<uint4 *>(smem + P::OFF_BF);
+    float *INV = reinterpret_cast<float *>(smem + P::OFF_INV);
+    float *CMAX = reinterpret_cast<float *>(smem + P::OFF_MAX);
+
+    // MMA warps: A-fragment entries (g, 2t), (g + 8, 2t), (g, 2t + 8),
+    // (g + 8, 2t + 8) of each k tile of the warp's row tile
+    uint32_t tab[2 * KT];
+    if (warp < P::MT) {
+        uint32_t *scratch = reinterpret_cast<uint32_t *>(smem) + (size_t)warp * 2 * KT * 32 + lane;
+#pragma unroll 1
+        for (int kt = 0; kt < KT; kt++) {
+            const int r0 = 16 * warp + g, c0 = 16 * kt + 2 * t;
+            scratch[(2 * kt) * 32] = sh_entry<NZ>(r0, c0) | (sh_entry<NZ>(r0 + 8, c0) << 16);
+            scratch[(2 * kt + 1) * 32] = sh_entry<NZ>(r0, c0 + 8) | (sh_entry<NZ>(r0 + 8, c0 + 8) << 16);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 2 * KT; j++) tab[j] = scratch[j * 32];
+    }
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int i = 0; i < 2; i++) {
+            mbar_init(b_full + 8 * i, 1);
+            mbar_init(b_sempty + 8 * i, 32 * P::MT);
+            mbar_init(b_bfull + 8 * i, 32 * P::NSPLIT);
+            mbar_init(b_bempty + 8 * i, 32 * P::MT);
+            mbar_init(b_max + 8 * i, 32 * P::NSPLIT);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp < P::MT) {
+        // ---- MMA warp: row tile mt
+        const int mt = warp;
+        // z rows: the -A^T tiles of the x and y columns take the sign
+        const bool zrows = (16 * mt) / NZ == 2;
+        for (int it = 0, q = blockIdx.x; q < Q; q += gridDim.x, it++) {
+            const int s = it & 1;
+            const uint32_t par = (it >> 1) & 1;
+            if (!ws_wait_warp(b_full + 8 * s, par, abort, err) || !ws_wait_warp(b_bfull + 8 * s, par, abort, err))
+                break;
+            const uint2 *Gq = reinterpret_cast<const uint2 *>(smem + s * P::G_BYTES);
+            const uint4 *bfr = BFRAG + (size_t)s * (P::BF_BYTES / 16) + lane;
+            // T1 = Gr Xr, T2 = Gi Xi, T3 = Gr Xi, T4 = Gi Xr, even and odd k tiles
+            float acc[2][4][4];
+#pragma unroll
+            for (int kt = 0; kt < KT; kt++) {
+                const uint32_t flip = (zrows && (16 * kt) / NZ < 2) ? 0x80008000u : 0u;
+                // B fragments [Xr, Xi][hi b0, hi b1, lo b0, lo b1]; the sign
+                // flips both FP16 halves (the split commutes with it)
+                uint32_t bf[2][4];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const uint4 f = bfr[(kt * 2 + h) * 32];
+                    bf[h][0] = f.x ^ flip;
+                    bf[h][1] = f.y ^ flip;
+                    bf[h][2] = f.z ^ flip;
+                    bf[h][3] = f.w ^ flip;
+                }
+                // [Gr hi, Gr lo, Gi hi, Gi lo][a0..a3]
+                uint32_t af[4][4];
+                const uint32_t t0 = tab[2 * kt], t1 = tab[2 * kt + 1];
+                const uint32_t ent[4] = {t0 & 0xffffu, t0 >> 16, t1 & 0xffffu, t1 >> 16};
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const uint32_t off = ent[e] & 0x7fffu, nb = (ent[e] & 0x8000u) ? 4u : 1u;
+                    const uint2 u = Gq[off], w = Gq[off ^ nb];
+                    af[0][e] = __byte_perm(u.x, w.x, 0x5410);
+                    af[2][e] = __byte_perm(u.x, w.x, 0x7632);
+                    af[1][e] = __byte_perm(u.y, w.y, 0x5410);
+                    af[3][e] = __byte_perm(u.y, w.y, 0x7632);
+                }
+                float (*ac)[4] = acc[kt & 1];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int ai = (j == 0 || j == 2) ? 0 : 2, bi = (j == 0 || j == 3) ? 0 : 1;
+                    if (kt < 2) mma_f16_zero(ac[j], af[ai], bf[bi][0], bf[bi][1]);
+                    else mma_f16(ac[j], af[ai], bf[bi][0], bf[bi][1]);
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int ai = (j == 0 || j == 2) ? 0 : 2, bi = (j == 0 || j == 3) ? 0 : 1;
+                    mma_f16(ac[j], af[ai], bf[bi][2], bf[bi][3]);
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int ai = (j == 0 || j == 2) ? 1 : 3, bi = (j == 0 || j == 3) ? 0 : 1;
+                    mma_f16(ac[j], af[ai], bf[bi][0], bf[bi][1]);
+                }
+            }
+            // undo the scales of accumulator columns 2t and 2t + 1
+            const float inv0 = INV[s * 8 + 2 * t], inv1 = INV[s * 8 + 2 * t + 1];
+            mbar_arrive(b_sempty + 8 * s);
+            mbar_arrive(b_bempty + 8 * s);
+            const int a = (int)((unsigned)q / (unsigned)(ny + 1)), bq = q - a * (ny + 1);
+            const int nkx = (a == 0 || a == nx) ? 1 : 2;
+            const int nky = (bq == 0 || bq == ny) ? 1 : 2;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                // rows g (c < 2) and g + 8 of the tile, column 2t + (c & 1):
+                // mirror point col & 3, source col >> 2
+                const int row = 16 * mt + g + 8 * (c >> 1);
+                const int col = 2 * t + (c & 1), v = col & 3, r = col >> 2;
+                const int mx = v >> 1, my = v & 1;
+                if (mx < nkx && my < nky) {
+                    const float f = (c & 1) ? inv1 : inv0;
+                    const float t1 = acc[0][0][c] + acc[1][0][c], t2 = acc[0][1][c] + acc[1][1][c];
+                    const float t3 = acc[0][2][c] + acc[1][2][c], t4 = acc[0][3][c] + acc[1][3][c];
+                    float2 val = make_float2((t1 - t2) * f, (t3 + t4) * f);
+                    const int comp = row / NZ;
+                    if ((comp == 0 && mx) || (comp == 1 && my)) val = make_float2(-val.x, -val.y);
+                    const long pt = (long)(mx ? 2 * nx - a : a) * n1 + (my ? 2 * ny - bq : bq);
+                    buf[pt * B + (long)(rhs0 + r) * R + row] = val;
+                }
+            }
+        }
+    } else if (warp < P::PRODUCER) {
+        // ---- split warp hh: k tiles hh, hh + NSPLIT, ... of every column
+        const int hh = warp - P::MT;
+        const int bv = g & 3, brs = g >> 2, bmx = bv >> 1, bmy = bv & 1;
+        for (int it = 0, q = blockIdx.x; q < Q; q += gridDim.x, it++) {
+            const int s = it & 1;
+            const uint32_t par = (it >> 1) & 1;
+            const int a = (int)((unsigned)q / (unsigned)(ny + 1)), bq = q - a * (ny + 1);
+            const int nkx = (a == 0 || a == nx) ? 1 : 2;
+            const int nky = (bq == 0 || bq == ny) ? 1 : 2;
+            const bool bpresent = bmx < nkx && bmy < nky;
+            // this lane's column: mirror point bv, source brs; rows
+            // 16 kt + 2t, +1 and 16 kt + 2t + 8, +9 with the D_p sign of
+            // their component (loads issued before the buffer wait)
+            float4 xv[P::KPS][2];
+            if (bpresent) {
+                const long pt = (long)(bmx ? 2 * nx - a : a) * n1 + (bmy ? 2 * ny - bq : bq);
+                const float4 *xcol = reinterpret_cast<const float4 *>(buf + pt * B + (long)(rhs0 + brs) * R);
+#pragma unroll
+                for (int i = 0; i < P::KPS; i++) {
+                    const int kt = hh + P::NSPLIT * i;
+                    if (kt < KT) {
+                        xv[i][0] = xcol[8 * kt + t];
+                        xv[i][1] = xcol[8 * kt + 4 + t];
+                    }
+                }
+            }
+            if (it >= 2 && !ws_wait_warp(b_bempty + 8 * s, par ^ 1u, abort, err)) break;
+            float m = 0.f;
+#pragma unroll
+            for (int i = 0; i < P::KPS; i++) {
+                const int kt = hh + P::NSPLIT * i;
+                if (kt >= KT) continue;
+                if (!bpresent) {
+                    xv[i][0] = xv[i][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    continue;
+                }
+                const int comp = (16 * kt) / NZ;
+                if ((comp == 0 && bmx) || (comp == 1 && bmy)) {
+#pragma unroll
+                    for (int h = 0; h < 2; h++)
+                        xv[i][h] = make_float4(-xv[i][h].x, -xv[i][h].y, -xv[i][h].z, -xv[i][h].w);
+                }
+#pragma unroll
+                for (int h = 0; h < 2; h++)
+                    m = fmaxf(m, fmaxf(fmaxf(fabsf(xv[i][h].x), fabsf(xv[i][h].y)),
+                                       fmaxf(fabsf(xv[i][h].z), fabsf(xv[i][h].w))));
+            }
+            // one scale per column over all its rows: the split warps'
+            // maxima meet in shared memory
+            m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+            m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
+            if (t == 0) CMAX[(s * P::NSPLIT + hh) * 8 + g] = m;
+            mbar_arrive(b_max + 8 * s);
+            if (!ws_wait_warp(b_max + 8 * s, par, abort, err)) break;
+            float mc = 0.f;
+#pragma unroll
+            for (int h = 0; h < P::NSPLIT; h++) mc = fmaxf(mc, CMAX[(s * P::NSPLIT + h) * 8 + g]);
+            const float scB = pow2_scale(mc, 13);
+            uint4 *bfw = BFRAG + (size_t)s * (P::BF_BYTES / 16) + lane;
+#pragma unroll
+            for (int i = 0; i < P::KPS; i++) {
+                const int kt = hh + P::NSPLIT * i;
+                if (kt >= KT) continue;
+                // [Xr, Xi] x [hi b0, hi b1, lo b0, lo b1]
+                uint4 fr, fi;
+                split_h2(xv[i][0].x * scB, xv[i][0].z * scB, fr.x, fr.z);
+                split_h2(xv[i][1].x * scB, xv[i][1].z * scB, fr.y, fr.w);
+                split_h2(xv[i][0].y * scB, xv[i][0].w * scB, fi.x, fi.z);
+                split_h2(xv[i][1].y * scB, xv[i][1].w * scB, fi.y, fi.w);
+                bfw[(kt * 2) * 32] = fr;
+                bfw[(kt * 2 + 1) * 32] = fi;
+            }
+            if (hh == 0 && t == 0) INV[s * 8 + g] = ginv / scB;
+            mbar_arrive(b_bfull + 8 * s);
+        }
+    } else if (lane == 0) {
+        // ---- producer: the Green block of each point into a free stage
+        int issued = 0;
+        for (int it = 0, q = blockIdx.x; q < Q; q += gridDim.x, it++) {
+            const int s = it & 1;
+            if (it >= 2 && !ws_wait(b_sempty + 8 * s, ((it >> 1) + 1) & 1, abort, err)) break;
+            // the stage was read through the generic proxy (and stage 0
+            // held the offset scratch)
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            bar_expect(b_full + 8 * s, P::G_BYTES);
+            bulk_g2s(sG + s * P::G_BYTES, G + (long)q * P::BS, P::G_BYTES, b_full + 8 * s);
+            issued = it + 1;
+        }
+        // no copy in flight when the block exits (bounded)
+        for (int j = issued > 2 ? issued - 2 : 0; j < issued; j++)
+            mbar_wait_ns(b_full + 8 * (j & 1), (j >> 1) & 1, kWait);
+    }
+}
+
 template <int NZ>
 void launch_sh(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err, cudaStream_t s, int nsm) {
     using P = Sh<NZ>;
@@ -1060,6 +1373,17 @@ void launch_sh(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err
     EGX_CHECK(Q < (1L << 31), EGX_ERR_INVALID, "sub-block contraction: (nx + 1)(ny + 1) must be below 2^31");
     const unsigned grid = (unsigned)std::min<long>(Q, nsm);
     k_contract_sh<NZ><<<grid, P::THREADS, P::SMEM, s>>>(buf, G, d.nx, d.ny, d.B, rhs0, err);
+    EGX_CUDA(cudaGetLastError());
+}
+
+template <int NZ>
+void launch_ws(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err, cudaStream_t s, int nsm) {
+    using P = Ws<NZ>;
+    raise_smem_limit((const void *)k_contract_ws<NZ>, P::SMEM);
+    const long Q = (long)(d.nx + 1) * (d.ny + 1);
+    EGX_CHECK(Q < (1L << 31), EGX_ERR_INVALID, "sub-block contraction: (nx + 1)(ny + 1) must be below 2^31");
+    const unsigned grid = (unsigned)std::min<long>(Q, nsm);
+    k_contract_ws<NZ><<<grid, P::THREADS, P::SMEM, s>>>(buf, G, d.nx, d.ny, d.B, rhs0, err);
     EGX_CUDA(cudaGetLastError());
 }
 
@@ -1086,16 +1410,18 @@ void launch_sb(float2 *buf, const float2 *G, const OpDims &d, int rhs0, int *err
 template <int NZ>
 void launch_nz(float2 *buf, const float2 *G, const OpDims &d, int *err, cudaStream_t s, int nsm, long *launches) {
     // contract_variant: 1 k_contract_sb3 (TF32 split), 2 k_contract_sh
-    // (FP16 split), 0 the built-in choice: k_contract_sh (2.059 against
-    // 2.562 ms per two-source apply at 256x256x48; 2.249 for k_contract_sb3
-    // when the copy held plain complex64)
+    // (FP16 split, all warps in lockstep), 0 the built-in choice:
+    // k_contract_ws (FP16 split by role: 1.110 against 1.293 ms per
+    // two-source launch at 256x256x48)
     const int v = d.contract_variant;
     for (int r0 = 0; r0 < d.nrhs;) {
         if (d.nrhs - r0 >= 2) {
             if (v == 1)
                 launch_sb3<NZ, true>(buf, G, d, r0, err, s, nsm);
-            else
+            else if (v == 2)
                 launch_sh<NZ>(buf, G, d, r0, err, s, nsm);
+            else
+                launch_ws<NZ>(buf, G, d, r0, err, s, nsm);
             r0 += 2;
         } else {
             launch_sb<NZ, 1>(buf, G, d, r0, err, s, nsm);
