@@ -66,10 +66,10 @@ METRIC_PLAIN = "MT solves/s, plain complex128 method (FGMRES(20)+GMRES(10), tol 
 
 # DRAM bytes (read + write) of one launch of the complex64 contraction at
 # 256x256x48, by right-hand sides per launch, measured by ncu at 128x128x48
-# (16,641 stored points) and scaled by the algorithmic bytes, which grow with
-# the stored points. One: 1.4262 GB x 5.6765 / 1.4290; two (k_contract_sb3):
-# 1.5719 GB x 6.2805 / 1.5800.
-CONTRACT_TRAFFIC_BYTES = {1: 5.665e9, 2: 6.248e9}
+# (16,641 stored points) and scaled by the stored bytes, which grow with the
+# stored points. One: 1.4262 GB x 5.6765 / 1.4290; two (k_contract_ws):
+# 1.5739 GB x 6.2805 / 1.5800.
+CONTRACT_TRAFFIC_BYTES = {1: 5.665e9, 2: 6.256e9}
 
 # Operator applications and outer iterations per polarisation of the plain
 # reference algorithm on the seed-1 model at each of its frequencies,
