@@ -629,9 +629,8 @@ int egx_tune_apply(egx_ctx *ctx, int nrhs, int reps, double *ms_out) {
         int bt = 0, bv = 0;
         // three contraction kernels to choose from in either Green layout:
         // packed (tensor-core, TMA-staged CUDA-core, generic) or sub-block
-        // for nz in 16, 32, 48 (built-in, k_contract_sb3 with the reduction
-        // on the first MT warps, k_contract_sb3 with it spread over the
-        // warps that have the fewest column tiles)
+        // for nz in 16, 32, 48 (built-in FP16 split by role, TF32 split,
+        // FP16 split in lockstep)
         const int nvar = 3;
         for (int tile = 0; tile < 3; tile++)
             for (int var = 0; var < nvar; var++) {

@@ -136,9 +136,9 @@ int egx_graph_stats(egx_ctx *ctx, long *replays, long *nodes);
  * for every kernel variant -- the FFT passes' column tile (0 built-in per
  * pass, 1 64-byte, 2 128-byte) x the contraction kernel: for the packed
  * Green layout 0 built-in order, 1 TMA-staged CUDA-core, 2 generic; for the
- * sub-block layout of nz in {16, 32, 48} 0 built-in (FP16 split), 1 TF32
- * split, 2 FP16 split -- keeps the fastest for the context's later
- * complex64 applies, and writes the mean ms per apply to
+ * sub-block layout of nz in {16, 32, 48} 0 built-in (FP16 split, warps by
+ * role), 1 TF32 split, 2 FP16 split in lockstep -- keeps the fastest for the
+ * context's later complex64 applies, and writes the mean ms per apply to
  * ms_out[tile * 3 + variant] (9 doubles; may be NULL). The results agree to
  * complex64 rounding whatever the choice. */
 int egx_tune_apply(egx_ctx *ctx, int nrhs, int reps, double *ms_out);

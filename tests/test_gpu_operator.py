@@ -90,14 +90,15 @@ def test_apply_small_matches_oracle(egx_ctx, small_case, op_type):
     g.free()
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2])
 @pytest.mark.parametrize("nz", [16, 32, 48])
 def test_c64_subblock_apply_matches_oracle(egx_ctx, nz, variant):
     """complex64 apply on the sub-block Green layout (nz in {16, 32, 48}),
     one to three right-hand sides (passes of two and one), ragged edges
     (nx != ny, the kx = 0, nx and ky = 0, ny points with fewer mirrors),
-    with the two-source passes on the TF32-split (variant 1) and the
-    FP16-split (variant 2) tensor-core kernels."""
+    with the two-source passes on the built-in FP16-split kernel by role
+    (variant 0), the TF32-split (variant 1) and the FP16-split lockstep
+    (variant 2) tensor-core kernels."""
     from extreme_gb300.model import freq_to_omega, scaled_model
     m = scaled_model(10, 6, nz, seed=3)
     f = m.frequencies[2]
