@@ -41,10 +41,11 @@
 //    entries recombined to complex64 first, and k_contract_sb<NZ, 1> for one
 //    right-hand side.
 //
-// Per stored point: one TMA bulk copy of the block and one per present
-// right-hand-side segment into one of two stages, issued two points ahead
-// and completing on the stage's mbarrier (waits bounded to 2 s; on expiry
-// EGX_ERR_TIMEOUT is recorded in *err and the kernel returns).
+// Per stored point: one TMA bulk copy of the block (and, in the lockstep
+// and TF32 kernels, one per present right-hand-side segment) into one of
+// two stages, issued two points ahead and completing on the stage's
+// mbarrier (waits bounded to 2 s; on expiry EGX_ERR_TIMEOUT is recorded in
+// *err and the kernel returns).
 #include <cuda_fp16.h>
 
 #include <algorithm>
