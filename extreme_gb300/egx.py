@@ -416,8 +416,8 @@ class Context:
             e, h = out
             shape = (nsrc, model.nx, model.ny, 3)
             for a in (e, h):
-                if a.dtype != np.complex128 or not a.flags.c_contiguous or a.size != int(np.prod(shape)):
-                    raise ValueError("out arrays must be C-contiguous complex128 of %s" % (shape,))
+                if a.dtype != np.complex128 or not a.flags.c_contiguous or a.shape != shape:
+                    raise ValueError("out arrays must be C-contiguous complex128 of shape %s" % (shape,))
         else:
             e = np.empty((nsrc, model.nx, model.ny, 3), np.complex128)
             h = np.empty_like(e)
